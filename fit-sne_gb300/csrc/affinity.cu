@@ -1,0 +1,536 @@
+// Input-similarity kernels (see affinity.cuh).
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "affinity.cuh"
+#include "knn.cuh"
+#include "sort.cuh"
+
+namespace fitsne {
+namespace {
+
+#define ACK(x)                                                          \
+    do {                                                                \
+        cudaError_t e__ = (x);                                          \
+        if (e__ != cudaSuccess) {                                       \
+            err = std::string(#x) + ": " + cudaGetErrorString(e__);     \
+            return -10;                                                 \
+        }                                                               \
+    } while (0)
+
+// ---------------------------------------------------------------------------------
+// X preparation
+__global__ void k_col_partial(const double *__restrict__ X, int N, int D, int rows_per_block,
+                              double *__restrict__ part) {
+    // part[block * D + d] = sum over this block's rows of X[:, d]
+    const int r0 = blockIdx.x * rows_per_block;
+    const int r1 = min(N, r0 + rows_per_block);
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        double s = 0.0;
+        for (int r = r0; r < r1; ++r) s += X[(size_t) r * D + d];
+        part[(size_t) blockIdx.x * D + d] = s;
+    }
+}
+
+__global__ void k_col_finish(const double *__restrict__ part, int nblk, int D, int N, double *__restrict__ mean) {
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nblk; ++b) s += part[(size_t) b * D + d];
+        mean[d] = s / (double) N;
+    }
+}
+
+__global__ void k_center_absmax(double *__restrict__ X, size_t n, int D, const double *__restrict__ mean,
+                                unsigned long long *__restrict__ amax) {
+    double m = 0.0;
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < n; e += (size_t) gridDim.x * blockDim.x) {
+        const double v = X[e] - mean[e % D];
+        X[e] = v;
+        m = fmax(m, fabs(v));
+    }
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    // non-negative doubles order like their bit patterns
+    if ((threadIdx.x & 31) == 0) atomicMax(amax, (unsigned long long) __double_as_longlong(m));
+}
+
+__global__ void k_scale(double *__restrict__ X, size_t n, const unsigned long long *__restrict__ amax) {
+    const double s = __longlong_as_double((long long) *amax);
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < n; e += (size_t) gridDim.x * blockDim.x)
+        X[e] /= s;
+}
+
+// ---------------------------------------------------------------------------------
+// perplexity calibration, one thread per row, sums in the reference's order
+// Re-evaluates P for the beta at which the reference stopped.  The reference computes P
+// inside the loop before testing, so P corresponds to the beta of the last evaluation;
+// this helper reproduces that beta and writes the normalised row.
+__device__ double calibrate_row(const double *__restrict__ d, double *__restrict__ p, int K, double perplexity,
+                                double sigma) {
+    double beta_eval;
+    if (perplexity > 0) {
+        double min_beta = -DBL_MAX, max_beta = DBL_MAX;
+        const double tol = 1e-5;
+        const double logU = log(perplexity);
+        bool found = false;
+        int iter = 0;
+        double beta = 1.0;
+        beta_eval = beta;
+        while (!found && iter < 200) {
+            beta_eval = beta;
+            double sum_P = DBL_MIN, H = 0.0;
+            for (int m = 0; m < K; ++m) {
+                const double e = exp(-beta * d[m]);
+                sum_P += e;
+                H += beta * (d[m] * e);
+            }
+            H = (H / sum_P) + log(sum_P);
+            const double Hdiff = H - logU;
+            if (Hdiff < tol && -Hdiff < tol) {
+                found = true;
+            } else if (Hdiff > 0) {
+                min_beta = beta;
+                if (max_beta == DBL_MAX || max_beta == -DBL_MAX)
+                    beta *= 2.0;
+                else
+                    beta = (beta + max_beta) / 2.0;
+            } else {
+                max_beta = beta;
+                if (min_beta == -DBL_MAX || min_beta == DBL_MAX)
+                    beta /= 2.0;
+                else
+                    beta = (beta + min_beta) / 2.0;
+            }
+            iter++;
+        }
+        // P of the reference is the row evaluated at beta_eval; the returned beta is the
+        // updated one when the loop ran out of iterations (as in the reference)
+        double sum_P = DBL_MIN;
+        for (int m = 0; m < K; ++m) {
+            p[m] = exp(-beta_eval * d[m]);
+            sum_P += p[m];
+        }
+        for (int m = 0; m < K; ++m) p[m] /= sum_P;
+        return beta;
+    }
+    beta_eval = 1 / (2 * sigma * sigma);
+    double sum_P = DBL_MIN;
+    for (int m = 0; m < K; ++m) {
+        p[m] = exp(-beta_eval * d[m]);
+        sum_P += p[m];
+    }
+    for (int m = 0; m < K; ++m) p[m] /= sum_P;
+    return beta_eval;
+}
+
+__global__ void k_calibrate(const double *__restrict__ dist, int stride, int offset, double *__restrict__ P,
+                            double *__restrict__ tmp, int nrows, int K, double perplexity, double sigma,
+                            const double *__restrict__ list, int list_len, double *__restrict__ beta_out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    const double *d = dist + (size_t) r * stride + offset;
+    double *p = P + (size_t) r * K;
+    double beta;
+    if (perplexity != 0) {
+        beta = calibrate_row(d, p, K, perplexity, sigma);
+    } else {
+        double *t = tmp + (size_t) r * K;
+        beta = calibrate_row(d, p, K, list[0], sigma);
+        for (int m = 1; m < list_len; ++m) {
+            beta = calibrate_row(d, t, K, list[m], sigma);
+            for (int i = 0; i < K; ++i) p[i] += t[i];
+        }
+        for (int i = 0; i < K; ++i) p[i] /= list_len;
+    }
+    if (beta_out) beta_out[r] = beta;
+}
+
+__global__ void k_knn_to_csr(const uint32_t *__restrict__ idx, int N, int K, uint32_t *__restrict__ row,
+                             uint32_t *__restrict__ col) {
+    const size_t n = (size_t) N * K;
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < n; e += (size_t) gridDim.x * blockDim.x) {
+        const size_t r = e / K, m = e % K;
+        col[e] = idx[r * (K + 1) + m + 1];
+    }
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r <= N; r += gridDim.x * blockDim.x) row[r] = (uint32_t) r * K;
+}
+
+// ---------------------------------------------------------------------------------
+// symmetrisation helpers
+__global__ void k_row_src(const uint32_t *__restrict__ row, int N, uint32_t *__restrict__ src) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x)
+        for (uint32_t e = row[r]; e < row[r + 1]; ++e) src[e] = (uint32_t) r;
+}
+
+// per-row copy of (col, position) sorted by col (insertion sort; rows are short)
+__global__ void k_row_sorted(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col, int N,
+                             uint32_t *__restrict__ scol, uint32_t *__restrict__ spos) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        const uint32_t a = row[r], b = row[r + 1];
+        for (uint32_t e = a; e < b; ++e) {
+            const uint32_t c = col[e];
+            uint32_t k = e;
+            while (k > a && scol[k - 1] > c) {
+                scol[k] = scol[k - 1];
+                spos[k] = spos[k - 1];
+                --k;
+            }
+            scol[k] = c;
+            spos[k] = e;
+        }
+    }
+}
+
+// position of c in row a (sorted copy), or 0xffffffff
+__device__ __forceinline__ uint32_t find_in_row(const uint32_t *__restrict__ row, const uint32_t *__restrict__ scol,
+                                                const uint32_t *__restrict__ spos, uint32_t a, uint32_t c) {
+    uint32_t lo = row[a], hi = row[a + 1];
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t v = scol[mid];
+        if (v < c)
+            lo = mid + 1;
+        else if (v > c)
+            hi = mid;
+        else
+            return spos[mid];
+    }
+    return 0xffffffffu;
+}
+
+__global__ void k_iota(uint32_t *__restrict__ v, size_t n) {
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < n; e += (size_t) gridDim.x * blockDim.x)
+        v[e] = (uint32_t) e;
+}
+
+__global__ void k_count_in(const uint32_t *__restrict__ col, size_t nnz, uint32_t *__restrict__ indeg) {
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < nnz; e += (size_t) gridDim.x * blockDim.x)
+        atomicAdd(&indeg[col[e]], 1u);
+}
+
+// Output row r: incoming n < r (ascending), r's own entries in list order except those
+// mirrored earlier, incoming n > r that r does not list (ascending)  (tsne.cpp:1772-1811).
+template <bool FILL>
+__global__ void k_sym_rows(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                           const double *__restrict__ val, const uint32_t *__restrict__ scol,
+                           const uint32_t *__restrict__ spos, const uint32_t *__restrict__ toff,
+                           const uint32_t *__restrict__ tedge, const uint32_t *__restrict__ src, int N,
+                           uint32_t *__restrict__ count, const uint32_t *__restrict__ srow,
+                           uint32_t *__restrict__ ocol, double *__restrict__ oval) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        uint32_t o = FILL ? srow[r] : 0u;
+        uint32_t c0 = 0;
+        const uint32_t ur = (uint32_t) r;
+        // first group: incoming n < r
+        for (uint32_t t = toff[r]; t < toff[r + 1]; ++t) {
+            const uint32_t e = tedge[t];
+            const uint32_t n = src[e];
+            if (n >= ur) break;
+            if (FILL) {
+                const uint32_t m = find_in_row(row, scol, spos, ur, n);
+                ocol[o] = n;
+                oval[o] = (m != 0xffffffffu) ? (val[e] + val[m]) / 2.0 : val[e] / 2.0;
+                ++o;
+            }
+            ++c0;
+        }
+        // middle: own entries
+        for (uint32_t e = row[r]; e < row[r + 1]; ++e) {
+            const uint32_t c = col[e];
+            const uint32_t m = find_in_row(row, scol, spos, c, ur);
+            if (m != 0xffffffffu && c < ur) continue;
+            if (FILL) {
+                ocol[o] = c;
+                oval[o] = (m != 0xffffffffu) ? (val[e] + val[m]) / 2.0 : val[e] / 2.0;
+                ++o;
+            }
+            ++c0;
+        }
+        // last group: incoming n > r not listed by r
+        for (uint32_t t = toff[r]; t < toff[r + 1]; ++t) {
+            const uint32_t e = tedge[t];
+            const uint32_t n = src[e];
+            if (n <= ur) continue;
+            if (find_in_row(row, scol, spos, ur, n) != 0xffffffffu) continue;
+            if (FILL) {
+                ocol[o] = n;
+                oval[o] = val[e] / 2.0;
+                ++o;
+            }
+            ++c0;
+        }
+        if (!FILL) count[r] = c0;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+__global__ void k_sum_part(const double *__restrict__ v, size_t n, double *__restrict__ part) {
+    __shared__ double sh[32];
+    double s = 0.0;
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < n; e += (size_t) gridDim.x * blockDim.x)
+        s += v[e];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int) (blockDim.x >> 5); ++w) t += sh[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_div(double *__restrict__ v, size_t n, const double *__restrict__ part, int nb) {
+    __shared__ double total;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int b = 0; b < nb; ++b) t += part[b];
+        total = t;
+    }
+    __syncthreads();
+    const double s = total;
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < n; e += (size_t) gridDim.x * blockDim.x)
+        v[e] /= s;
+}
+
+__global__ void k_row_sums_max(const uint32_t *__restrict__ row, const double *__restrict__ val, int N,
+                               unsigned long long *__restrict__ mx) {
+    double m = 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (uint32_t e = row[r]; e < row[r + 1]; ++e) s += val[e];
+        m = fmax(m, s);
+    }
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, (unsigned long long) __double_as_longlong(m));
+}
+
+int key_bits_for(int N) {
+    int b = 1;
+    while (b < 32 && (1u << b) < (unsigned) N) ++b;
+    return b;
+}
+
+}  // namespace
+
+void free_csr(DevCSR &P) {
+    cudaFree(P.row);
+    cudaFree(P.col);
+    cudaFree(P.val);
+    P.row = P.col = nullptr;
+    P.val = nullptr;
+    P.nnz = 0;
+}
+
+int prepare_X(const double *X_host, int N, int D, bool normalize, double **Xd_out, cudaStream_t st,
+              std::string &err) {
+    double *Xd = nullptr, *part = nullptr, *mean = nullptr;
+    unsigned long long *amax = nullptr;
+    const size_t n = (size_t) N * D;
+    ACK(cudaMalloc(&Xd, sizeof(double) * (n ? n : 1)));
+    ACK(cudaMemcpyAsync(Xd, X_host, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    const int rpb = 256;
+    const int nblk = (N + rpb - 1) / rpb;
+    ACK(cudaMalloc(&part, sizeof(double) * (size_t) nblk * D + 8));
+    ACK(cudaMalloc(&mean, sizeof(double) * D + 8));
+    ACK(cudaMalloc(&amax, sizeof(unsigned long long)));
+    ACK(cudaMemsetAsync(amax, 0, sizeof(unsigned long long), st));
+    k_col_partial<<<nblk, 64, 0, st>>>(Xd, N, D, rpb, part);
+    k_col_finish<<<1, 256, 0, st>>>(part, nblk, D, N, mean);
+    k_center_absmax<<<2048, 256, 0, st>>>(Xd, n, D, mean, amax);
+    if (normalize) k_scale<<<2048, 256, 0, st>>>(Xd, n, amax);
+    ACK(cudaGetLastError());
+    ACK(cudaStreamSynchronize(st));
+    cudaFree(part);
+    cudaFree(mean);
+    cudaFree(amax);
+    *Xd_out = Xd;
+    return 0;
+}
+
+int calibrate_rows(const double *dist, int stride, int offset, double *P, int nrows, int K, double perplexity,
+                   double sigma, int list_len, const double *list_host, double *beta, cudaStream_t st,
+                   std::string &err) {
+    double *list = nullptr, *tmp = nullptr;
+    if (perplexity == 0) {
+        if (list_len < 1 || !list_host) {
+            err = "perplexity 0 needs a perplexity list";
+            return -3;
+        }
+        ACK(cudaMalloc(&list, sizeof(double) * list_len));
+        ACK(cudaMemcpyAsync(list, list_host, sizeof(double) * list_len, cudaMemcpyHostToDevice, st));
+        ACK(cudaMalloc(&tmp, sizeof(double) * (size_t) nrows * K));
+    }
+    k_calibrate<<<(nrows + 127) / 128, 128, 0, st>>>(dist, stride, offset, P, tmp, nrows, K, perplexity, sigma, list,
+                                                      list_len, beta);
+    ACK(cudaGetLastError());
+    ACK(cudaStreamSynchronize(st));
+    cudaFree(list);
+    cudaFree(tmp);
+    return 0;
+}
+
+int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double perplexity, double sigma, int list_len,
+                               const double *list_host, DevCSR *out, cudaStream_t st, std::string &err,
+                               int *knn_rescanned) {
+    if (K < 1 || K + 1 > N) {
+        err = "K + 1 must not exceed the number of points";
+        return -3;
+    }
+    uint32_t *idx = nullptr;
+    double *dist = nullptr;
+    ACK(cudaMalloc(&idx, sizeof(uint32_t) * (size_t) N * (K + 1)));
+    ACK(cudaMalloc(&dist, sizeof(double) * (size_t) N * (K + 1)));
+    KnnStats ks;
+    const char *kerr = nullptr;
+    int rc = knn_exact(Xd, N, D, K + 1, idx, dist, st, &ks, &kerr);
+    if (rc) {
+        err = kerr ? kerr : "kNN failed";
+        cudaFree(idx);
+        cudaFree(dist);
+        return rc;
+    }
+    if (knn_rescanned) *knn_rescanned = ks.rows_rescanned;
+    DevCSR P;
+    P.N = N;
+    P.nnz = (size_t) N * K;
+    ACK(cudaMalloc(&P.row, sizeof(uint32_t) * (N + 1)));
+    ACK(cudaMalloc(&P.col, sizeof(uint32_t) * P.nnz));
+    ACK(cudaMalloc(&P.val, sizeof(double) * P.nnz));
+    k_knn_to_csr<<<4096, 256, 0, st>>>(idx, N, K, P.row, P.col);
+    ACK(cudaGetLastError());
+    rc = calibrate_rows(dist, K + 1, 1, P.val, N, K, perplexity, sigma, list_len, list_host, nullptr, st, err);
+    cudaFree(idx);
+    cudaFree(dist);
+    if (rc) {
+        free_csr(P);
+        return rc;
+    }
+    *out = P;
+    return 0;
+}
+
+int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::string &err) {
+    const int N = in.N;
+    const size_t nnz = in.nnz;
+    uint32_t *src = nullptr, *scol = nullptr, *spos = nullptr, *keys = nullptr, *tedge = nullptr, *kalt = nullptr,
+             *valt = nullptr, *indeg = nullptr, *toff = nullptr, *cnt = nullptr;
+    void *scratch = nullptr;
+    const size_t nz = nnz ? nnz : 1;
+    ACK(cudaMalloc(&src, sizeof(uint32_t) * nz));
+    ACK(cudaMalloc(&scol, sizeof(uint32_t) * nz));
+    ACK(cudaMalloc(&spos, sizeof(uint32_t) * nz));
+    ACK(cudaMalloc(&keys, sizeof(uint32_t) * nz));
+    ACK(cudaMalloc(&tedge, sizeof(uint32_t) * nz));
+    ACK(cudaMalloc(&kalt, sizeof(uint32_t) * nz));
+    ACK(cudaMalloc(&valt, sizeof(uint32_t) * nz));
+    ACK(cudaMalloc(&indeg, sizeof(uint32_t) * (N + 1)));
+    ACK(cudaMalloc(&toff, sizeof(uint32_t) * (N + 2)));
+    ACK(cudaMalloc(&cnt, sizeof(uint32_t) * (N + 1)));
+    const size_t scr = radix_sort_scratch_bytes(nz) + scan_scratch_bytes((size_t) N + 1);
+    ACK(cudaMalloc(&scratch, scr));
+    const int g = 2048;
+    k_row_src<<<(N + 255) / 256, 256, 0, st>>>(in.row, N, src);
+    k_row_sorted<<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, N, scol, spos);
+    // transpose: group edge ids by column, stable in edge order
+    ACK(cudaMemcpyAsync(keys, in.col, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToDevice, st));
+    k_iota<<<g, 256, 0, st>>>(tedge, nnz);
+    ACK(radix_sort_pairs(keys, tedge, kalt, valt, nnz, key_bits_for(N), scratch, st));
+    ACK(cudaMemsetAsync(indeg, 0, sizeof(uint32_t) * (N + 1), st));
+    k_count_in<<<g, 256, 0, st>>>(in.col, nnz, indeg);
+    ACK(exclusive_scan_u32(indeg, toff, (size_t) N, scratch, st));
+    k_sym_rows<false><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, cnt,
+                                                       nullptr, nullptr, nullptr);
+    DevCSR P;
+    P.N = N;
+    ACK(cudaMalloc(&P.row, sizeof(uint32_t) * (N + 1)));
+    ACK(exclusive_scan_u32(cnt, P.row, (size_t) N, scratch, st));
+    uint32_t total = 0;
+    ACK(cudaMemcpyAsync(&total, P.row + N, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    P.nnz = total;
+    ACK(cudaMalloc(&P.col, sizeof(uint32_t) * (total ? total : 1)));
+    ACK(cudaMalloc(&P.val, sizeof(double) * (total ? total : 1)));
+    k_sym_rows<true><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
+                                                      nullptr, P.row, P.col, P.val);
+    ACK(cudaGetLastError());
+    ACK(cudaStreamSynchronize(st));
+    cudaFree(src);
+    cudaFree(scol);
+    cudaFree(spos);
+    cudaFree(keys);
+    cudaFree(tedge);
+    cudaFree(kalt);
+    cudaFree(valt);
+    cudaFree(indeg);
+    cudaFree(toff);
+    cudaFree(cnt);
+    cudaFree(scratch);
+    *out = P;
+    return 0;
+}
+
+int normalize_device(DevCSR &P, double *sum, cudaStream_t st, std::string &err) {
+    const int nb = 1024;
+    double *part = nullptr;
+    ACK(cudaMalloc(&part, sizeof(double) * nb));
+    k_sum_part<<<nb, 256, 0, st>>>(P.val, P.nnz, part);
+    k_div<<<2048, 256, 0, st>>>(P.val, P.nnz, part, nb);
+    if (sum) {
+        std::vector<double> h(nb);
+        ACK(cudaMemcpyAsync(h.data(), part, sizeof(double) * nb, cudaMemcpyDeviceToHost, st));
+        ACK(cudaStreamSynchronize(st));
+        double t = 0.0;
+        for (double v : h) t += v;
+        *sum = t;
+    }
+    ACK(cudaStreamSynchronize(st));
+    cudaFree(part);
+    return 0;
+}
+
+int max_row_sum_device(const DevCSR &P, double *out, cudaStream_t st, std::string &err) {
+    unsigned long long *mx = nullptr;
+    ACK(cudaMalloc(&mx, sizeof(unsigned long long)));
+    ACK(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), st));
+    k_row_sums_max<<<(P.N + 255) / 256, 256, 0, st>>>(P.row, P.val, P.N, mx);
+    unsigned long long h = 0;
+    ACK(cudaMemcpyAsync(&h, mx, sizeof(h), cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    cudaFree(mx);
+    double d;
+    static_assert(sizeof(d) == sizeof(h), "size");
+    std::memcpy(&d, &h, sizeof(d));
+    *out = d;
+    return 0;
+}
+
+int csr_to_device(const uint32_t *row, const uint32_t *col, const double *val, int N, DevCSR *out, cudaStream_t st,
+                  std::string &err) {
+    DevCSR P;
+    P.N = N;
+    P.nnz = row[N];
+    ACK(cudaMalloc(&P.row, sizeof(uint32_t) * (N + 1)));
+    ACK(cudaMalloc(&P.col, sizeof(uint32_t) * (P.nnz ? P.nnz : 1)));
+    ACK(cudaMalloc(&P.val, sizeof(double) * (P.nnz ? P.nnz : 1)));
+    ACK(cudaMemcpyAsync(P.row, row, sizeof(uint32_t) * (N + 1), cudaMemcpyHostToDevice, st));
+    if (P.nnz) {
+        ACK(cudaMemcpyAsync(P.col, col, sizeof(uint32_t) * P.nnz, cudaMemcpyHostToDevice, st));
+        ACK(cudaMemcpyAsync(P.val, val, sizeof(double) * P.nnz, cudaMemcpyHostToDevice, st));
+    }
+    ACK(cudaStreamSynchronize(st));
+    *out = P;
+    return 0;
+}
+
+int csr_to_host(const DevCSR &P, uint32_t *row, uint32_t *col, double *val, cudaStream_t st, std::string &err) {
+    ACK(cudaMemcpyAsync(row, P.row, sizeof(uint32_t) * (P.N + 1), cudaMemcpyDeviceToHost, st));
+    if (P.nnz) {
+        ACK(cudaMemcpyAsync(col, P.col, sizeof(uint32_t) * P.nnz, cudaMemcpyDeviceToHost, st));
+        ACK(cudaMemcpyAsync(val, P.val, sizeof(double) * P.nnz, cudaMemcpyDeviceToHost, st));
+    }
+    ACK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+}  // namespace fitsne

@@ -1,0 +1,130 @@
+// Device-resident state of one embedding and the host loop that drives the kernels.
+//
+// Embedding<T> mirrors the gradient part of TSNE::run (src/tsne.cpp:437-577 of the
+// reference): per iteration it centres Y (zeroMean of the previous step), reads the
+// bounding square, builds the interpolation grid with the reference's box-count rule,
+// spreads, convolves, gathers, and applies the attraction + optimiser step in one pass.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "fftconv.cuh"
+#include "grad.cuh"
+
+namespace fitsne {
+
+// Optimiser schedule (arguments of TSNE::run that drive the iteration loop).
+struct Schedule {
+    int max_iter = 1000;
+    int stop_lying_iter = 250;
+    int mom_switch_iter = 250;
+    double momentum = 0.5;
+    double final_momentum = 0.8;
+    double learning_rate = 200.0;
+    double early_exag_coeff = 12.0;
+    int no_momentum_during_exag = 0;
+    int start_late_exag_iter = -1;
+    double late_exag_coeff = -1.0;
+    double max_step_norm = 5.0;
+};
+
+struct GridParams {
+    int nterms = 3;
+    double intervals_per_integer = 1.0;
+    int min_num_intervals = 50;
+    double df = 1.0;
+};
+
+// Per-stage device time of the last timed iteration (CUDA events), milliseconds.
+struct StageTimes {
+    float center = 0, spread = 0, conv = 0, gather = 0, attract = 0, total = 0;
+};
+
+template <typename T>
+class Embedding {
+   public:
+    typedef typename Cx<T>::t C;
+
+    Embedding();
+    ~Embedding();
+    Embedding(const Embedding &) = delete;
+    Embedding &operator=(const Embedding &) = delete;
+
+    // Uploads P (host CSR; val in FP64) and the initial Y (host, N x D row-major).
+    int init_host(int N, int D, const uint32_t *row, const uint32_t *col, const double *val, const double *Y0,
+                  const GridParams &gp, cudaStream_t st);
+    // Takes P already on the device (row/col u32, val FP64); the arrays are copied.
+    int init_device(int N, int D, const uint32_t *d_row, const uint32_t *d_col, const double *d_val,
+                    size_t nnz, const double *Y0_host, const GridParams &gp, cudaStream_t st);
+
+    // One gradient evaluation without update: dC (host, N x D) and Z.
+    int gradient(double *dC_host, double *sum_Q);
+    // One optimiser iteration with the given step parameters.
+    int step(const UpdateParams &p, bool first);
+    // KL divergence with the current Y, the Z of the last gradient, P scaled by exag.
+    int kl(double exag, double *out);
+    // KL with a caller-supplied Z (evaluateErrorFft with current_sum_Q set by the caller).
+    int kl_with_z(double exag, double z, double *out);
+    // Subtracts the pending mean and copies Y to the host.
+    int get_Y(double *Y_host);
+
+    // Runs iterations [it0, it1) of the reference schedule; costs may be null.
+    int run_schedule(const Schedule &s, int it0, int it1, double *costs, bool verbose);
+
+    void set_timing(bool on) { timing_ = on; }
+    const StageTimes &last_times() const { return times_; }
+    const GridGeom &last_geom() const { return geom_; }
+    int last_L() const { return L_; }
+    size_t nnz() const { return nnz_; }
+    int N() const { return N_; }
+    cudaStream_t stream() const { return st_; }
+    const std::string &error() const { return err_; }
+    // device pointers (for zero-copy consumers such as the no-allocation path)
+    const uint32_t *d_row() const { return row_; }
+    const uint32_t *d_col() const { return col_; }
+    const T *d_val() const { return val_; }
+    const T *d_Y() const { return Y_[cur_]; }
+
+   private:
+    int alloc_common(int N, int D, size_t nnz);
+    int prepare_grid();  // reads min/max (synchronises) and sizes the grid
+    int repulsion();     // spread + conv + gather
+    int fail(const char *what, cudaError_t e);
+
+    int N_ = 0, D_ = 0;
+    size_t nnz_ = 0;
+    GridParams gp_;
+    cudaStream_t st_ = nullptr;
+    uint32_t *row_ = nullptr, *col_ = nullptr;
+    T *val_ = nullptr;
+    T *Y_[2] = {nullptr, nullptr};
+    int cur_ = 0;
+    bool mean_pending_ = false;
+    T *uY_ = nullptr, *gains_ = nullptr, *rep_ = nullptr, *dC_ = nullptr;
+    Cell4<T> *grid_in_ = nullptr, *grid_out_ = nullptr;
+    size_t grid_cap_ = 0;
+    C *work_a_ = nullptr, *work_b_ = nullptr;
+    size_t wa_cap_ = 0, wb_cap_ = 0;
+    KSpec<T> *kspec_ = nullptr;
+    size_t ks_cap_ = 0;
+    std::map<int, C *> tw_;
+    RedScratch red_{};
+    double *red_mem_ = nullptr;
+    unsigned int *red_cnt_ = nullptr;
+    double *h_pin_ = nullptr;  // pinned: [min, max, z, kl]
+    GridGeom geom_{};
+    FftPlan plan_{};
+    int L_ = 0;
+    bool timing_ = false;
+    StageTimes times_;
+    cudaEvent_t ev_[6] = {};
+    std::string err_;
+};
+
+// Box-count rule of the reference (tsne.cpp:1065-1077 for 2-D, 663/774 for 1-D) and
+// the node layout of precompute_2d / precompute (nbodyfft.cpp:9-70, 251-307).
+GridGeom make_grid_geom(double mn, double mx, int D, const GridParams &gp);
+
+}  // namespace fitsne

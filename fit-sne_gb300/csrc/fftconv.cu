@@ -1,0 +1,541 @@
+// Shared-memory mixed-radix FFT convolution (see fftconv.cuh for the contract).
+//
+// 2-D data flow for one gradient evaluation (L = transform length, H = L/2 + 1):
+//   k_kernel_rows  : builds the 4 kernel fields row by row (rows with a signed offset in
+//                    (-M, M) only), r2c along the row, writes half spectra [4][L][H]
+//   k_kernel_cols  : column FFTs of the kernel half spectra -> compact KSpec[H][L]
+//   k_data_rows    : r2c of the M non-zero rows of the 4 spread fields -> [4][M][H]
+//   k_data_cols    : per column: forward FFT (rows >= M are the zero padding), spectral
+//                    products that form the 4 output fields, inverse FFT, keep rows < M
+//   k_data_rows_inv: c2r of the M kept rows, keep columns < M -> potential grid
+// Every pass keeps one or two whole transforms in shared memory; passes are Stockham
+// (self-sorting) with radix 4, 2, 3, 5 butterflies.
+#include <climits>
+
+#include "fftconv.cuh"
+
+namespace fitsne {
+
+bool make_fft_plan(int L, FftPlan *p) {
+    p->L = L;
+    p->nst = 0;
+    int n = L;
+    while (n % 4 == 0 && p->nst < 24) { p->radix[p->nst++] = 4; n /= 4; }
+    while (n % 2 == 0 && p->nst < 24) { p->radix[p->nst++] = 2; n /= 2; }
+    while (n % 3 == 0 && p->nst < 24) { p->radix[p->nst++] = 3; n /= 3; }
+    while (n % 5 == 0 && p->nst < 24) { p->radix[p->nst++] = 5; n /= 5; }
+    return n == 1 && L >= 2;
+}
+
+int smooth_even_at_least(int n) {
+    for (int m = n < 2 ? 2 : n;; ++m) {
+        if (m & 1) continue;
+        int k = m;
+        while (k % 2 == 0) k /= 2;
+        while (k % 3 == 0) k /= 3;
+        while (k % 5 == 0) k /= 5;
+        if (k == 1) return m;
+    }
+}
+
+namespace {
+
+template <typename C>
+FITSNE_D C twid(const C *__restrict__ tw, int j, bool inv) {
+    C w = tw[j];
+    return inv ? cconj(w) : w;
+}
+
+// small DFTs; forward uses exp(-2 pi i / R), inverse exp(+2 pi i / R)
+template <int R, typename C>
+struct Dft;
+
+template <typename C>
+struct Dft<2, C> {
+    static FITSNE_D void run(C *u, bool) {
+        C a = u[0], b = u[1];
+        u[0] = cadd(a, b);
+        u[1] = csub(a, b);
+    }
+};
+
+template <typename C>
+struct Dft<4, C> {
+    static FITSNE_D void run(C *u, bool inv) {
+        C a0 = cadd(u[0], u[2]), a1 = csub(u[0], u[2]);
+        C b0 = cadd(u[1], u[3]), b1 = csub(u[1], u[3]);
+        C jb1 = inv ? cmul_pi(b1) : cmul_mi(b1);
+        u[0] = cadd(a0, b0);
+        u[2] = csub(a0, b0);
+        u[1] = cadd(a1, jb1);
+        u[3] = csub(a1, jb1);
+    }
+};
+
+template <typename C>
+struct Dft<3, C> {
+    static FITSNE_D void run(C *u, bool inv) {
+        typedef decltype(u[0].x) T;
+        const T c = T(-0.5);
+        const T s = T(0.86602540378443864676372317075294);  // sin(2 pi / 3)
+        C t = cadd(u[1], u[2]);
+        C d = csub(u[1], u[2]);
+        C m = mkc(u[0].x + c * t.x, u[0].y + c * t.y);
+        // forward: y1 = m - i s d, y2 = m + i s d
+        C isd = mkc(-s * d.y, s * d.x);
+        u[0] = cadd(u[0], t);
+        if (!inv) {
+            u[1] = csub(m, isd);
+            u[2] = cadd(m, isd);
+        } else {
+            u[1] = cadd(m, isd);
+            u[2] = csub(m, isd);
+        }
+    }
+};
+
+template <typename C>
+struct Dft<5, C> {
+    static FITSNE_D void run(C *u, bool inv) {
+        typedef decltype(u[0].x) T;
+        const T c1 = T(0.30901699437494742410229341718282);   // cos(2 pi / 5)
+        const T s1 = T(0.95105651629515357211643933337938);   // sin(2 pi / 5)
+        const T c2 = T(-0.80901699437494742410229341718282);  // cos(4 pi / 5)
+        const T s2 = T(0.58778525229247312916870595463907);   // sin(4 pi / 5)
+        C a1 = cadd(u[1], u[4]), b1 = csub(u[1], u[4]);
+        C a2 = cadd(u[2], u[3]), b2 = csub(u[2], u[3]);
+        C m1 = mkc(u[0].x + c1 * a1.x + c2 * a2.x, u[0].y + c1 * a1.y + c2 * a2.y);
+        C m2 = mkc(u[0].x + c2 * a1.x + c1 * a2.x, u[0].y + c2 * a1.y + c1 * a2.y);
+        // n1 = s1 b1 + s2 b2 ; n2 = s2 b1 - s1 b2 ; forward y1 = m1 - i n1, y4 = m1 + i n1,
+        // y2 = m2 - i n2, y3 = m2 + i n2
+        C n1 = mkc(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
+        C n2 = mkc(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
+        C in1 = cmul_pi(n1), in2 = cmul_pi(n2);
+        u[0] = mkc(u[0].x + a1.x + a2.x, u[0].y + a1.y + a2.y);
+        if (!inv) {
+            u[1] = csub(m1, in1);
+            u[4] = cadd(m1, in1);
+            u[2] = csub(m2, in2);
+            u[3] = cadd(m2, in2);
+        } else {
+            u[1] = cadd(m1, in1);
+            u[4] = csub(m1, in1);
+            u[2] = cadd(m2, in2);
+            u[3] = csub(m2, in2);
+        }
+    }
+};
+
+// One Stockham butterfly: inputs i + r*T, twiddle exp(-+2 pi i r k / (p R)), outputs
+// (i - k) R + k + r p with k = i mod p.
+template <int R, typename C>
+FITSNE_D void bfly(const C *src, C *dst, int i, int T, int p, int tws, const C *__restrict__ tw, bool inv) {
+    const int k = i % p;
+    C u[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) u[r] = src[i + r * T];
+    if (k) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) u[r] = cmul(u[r], twid(tw, r * k * tws, inv));
+    }
+    Dft<R, C>::run(u, inv);
+    const int base = (i - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[base + r * p] = u[r];
+}
+
+// nf independent length-L transforms stored at a[f*L]; b is scratch of the same size.
+// Data must be visible to the whole block on entry.  Returns the buffer holding the
+// result (a or b).
+template <typename C>
+FITSNE_D C *fft_block(C *a, C *b, int nf, const FftPlan &pl, const C *__restrict__ tw, bool inv) {
+    const int L = pl.L;
+    C *src = a;
+    C *dst = b;
+    int p = 1;
+    for (int s = 0; s < pl.nst; ++s) {
+        const int R = pl.radix[s];
+        const int T = L / R;
+        const int tws = L / (p * R);
+        const int total = T * nf;
+        for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+            const int f = idx / T;
+            const int i = idx - f * T;
+            const C *sf = src + f * L;
+            C *df = dst + f * L;
+            if (R == 4)
+                bfly<4>(sf, df, i, T, p, tws, tw, inv);
+            else if (R == 2)
+                bfly<2>(sf, df, i, T, p, tws, tw, inv);
+            else if (R == 3)
+                bfly<3>(sf, df, i, T, p, tws, tw, inv);
+            else
+                bfly<5>(sf, df, i, T, p, tws, tw, inv);
+        }
+        __syncthreads();
+        C *t = src;
+        src = dst;
+        dst = t;
+        p *= R;
+    }
+    return src;
+}
+
+// kernel values at node offset (dx, dy) in node units, node spacing h
+template <typename T>
+FITSNE_D void kernel_vals_2d(int dx, int dy, T h, T df, int mode, T &k, T &gx, T &gy, T &hh) {
+    const T ex = T(dx) * h;
+    const T ey = T(dy) * h;
+    const T r2 = ex * ex + ey * ey;
+    if (mode == KERNEL_DF1) {
+        const T q = T(1) / (T(1) + r2);
+        k = q * q;
+        hh = k * r2;
+    } else {
+        const T base = T(1) + r2 / df;
+        k = pow(base, -(df + T(1)));
+        hh = pow(base, -df);
+    }
+    gx = k * ex;
+    gy = k * ey;
+}
+
+template <typename T>
+FITSNE_D void kernel_vals_1d(int d, T h, T df, int mode, T &k, T &g, T &hh) {
+    const T e = T(d) * h;
+    const T r2 = e * e;
+    if (mode == KERNEL_DF1) {
+        const T q = T(1) / (T(1) + r2);
+        k = q * q;
+        hh = k * r2;
+    } else {
+        const T base = T(1) + r2 / df;
+        k = pow(base, -(df + T(1)));
+        hh = pow(base, -df);
+    }
+    g = k * e;
+}
+
+// split the spectrum Z of (f + i g) into the half spectra of f and g at index kb
+template <typename C, typename T>
+FITSNE_D void unpack_r2c(const C *Zs, int L, int kb, C &F, C &G) {
+    C Z = Zs[kb];
+    C Zc = cconj(Zs[kb == 0 ? 0 : L - kb]);
+    F = cscale(cadd(Z, Zc), T(0.5));
+    G = cscale(cmul_mi(csub(Z, Zc)), T(0.5));
+}
+
+template <typename T>
+__global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
+                              typename Cx<T>::t *__restrict__ krow, T h, T df, int mode) {
+    typedef typename Cx<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = pl.L, H = L / 2 + 1;
+    C *bufa = reinterpret_cast<C *>(smem_raw);
+    C *bufb = bufa + 2 * L;
+    const int r = blockIdx.x;
+    const int a = (r < M) ? r : (L - (2 * M - 1 - r));
+    const int dx = (a < M) ? a : a - L;
+    for (int b = threadIdx.x; b < L; b += blockDim.x) {
+        T k = 0, gx = 0, gy = 0, hh = 0;
+        if (b < M || b > L - M) {
+            const int dy = (b < M) ? b : b - L;
+            kernel_vals_2d<T>(dx, dy, h, df, mode, k, gx, gy, hh);
+        }
+        bufa[b] = mkc(k, gx);
+        bufa[L + b] = mkc(gy, hh);
+    }
+    __syncthreads();
+    C *res = fft_block(bufa, bufb, 2, pl, tw, false);
+    for (int kb = threadIdx.x; kb < H; kb += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            C F, G;
+            unpack_r2c<C, T>(res + q * L, L, kb, F, G);
+            krow[((size_t) (2 * q) * L + a) * H + kb] = F;
+            krow[((size_t) (2 * q + 1) * L + a) * H + kb] = G;
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_kernel_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
+                              const typename Cx<T>::t *__restrict__ krow, KSpec<T> *__restrict__ kspec) {
+    typedef typename Cx<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = pl.L, H = L / 2 + 1;
+    C *spec = reinterpret_cast<C *>(smem_raw);
+    C *scratch = spec + 4 * L;
+    const int kb = blockIdx.x;
+    for (int f = 0; f < 4; ++f)
+        for (int a = threadIdx.x; a < L; a += blockDim.x) {
+            const bool valid = (a < M) || (a > L - M);
+            spec[f * L + a] = valid ? krow[((size_t) f * L + a) * H + kb] : mkc(T(0), T(0));
+        }
+    __syncthreads();
+    for (int f = 0; f < 4; ++f) {
+        C *res = fft_block(spec + f * L, scratch, 1, pl, tw, false);
+        if (res != spec + f * L) {
+            for (int a = threadIdx.x; a < L; a += blockDim.x) spec[f * L + a] = res[a];
+            __syncthreads();
+        }
+    }
+    const T s = T(1) / (T(L) * T(L));
+    for (int ka = threadIdx.x; ka < L; ka += blockDim.x) {
+        KSpec<T> e;
+        e.k = spec[ka].x * s;
+        e.gx = spec[L + ka].y * s;
+        e.gy = spec[2 * L + ka].y * s;
+        e.h = spec[3 * L + ka].x * s;
+        kspec[(size_t) kb * L + ka] = e;
+    }
+}
+
+template <typename T>
+__global__ void k_data_rows(const Cell4<T> *__restrict__ grid, int M, FftPlan pl,
+                            const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ d1) {
+    typedef typename Cx<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = pl.L, H = L / 2 + 1;
+    C *bufa = reinterpret_cast<C *>(smem_raw);
+    C *bufb = bufa + 2 * L;
+    const int a = blockIdx.x;
+    for (int b = threadIdx.x; b < L; b += blockDim.x) {
+        Cell4<T> v;
+        if (b < M)
+            v = grid[(size_t) a * M + b];
+        else
+            v.a = v.b = v.c = v.d = T(0);
+        bufa[b] = mkc(v.a, v.b);
+        bufa[L + b] = mkc(v.c, v.d);
+    }
+    __syncthreads();
+    C *res = fft_block(bufa, bufb, 2, pl, tw, false);
+    for (int kb = threadIdx.x; kb < H; kb += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            C F, G;
+            unpack_r2c<C, T>(res + q * L, L, kb, F, G);
+            d1[((size_t) (2 * q) * M + a) * H + kb] = F;
+            d1[((size_t) (2 * q + 1) * M + a) * H + kb] = G;
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_data_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
+                            const typename Cx<T>::t *__restrict__ d1, const KSpec<T> *__restrict__ kspec,
+                            typename Cx<T>::t *__restrict__ d2, int mode) {
+    typedef typename Cx<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = pl.L, H = L / 2 + 1;
+    C *spec = reinterpret_cast<C *>(smem_raw);
+    C *scratch = spec + 4 * L;
+    const int kb = blockIdx.x;
+    for (int f = 0; f < 4; ++f)
+        for (int a = threadIdx.x; a < L; a += blockDim.x)
+            spec[f * L + a] = (a < M) ? d1[((size_t) f * M + a) * H + kb] : mkc(T(0), T(0));
+    __syncthreads();
+    for (int f = 0; f < 4; ++f) {
+        C *res = fft_block(spec + f * L, scratch, 1, pl, tw, false);
+        if (res != spec + f * L) {
+            for (int a = threadIdx.x; a < L; a += blockDim.x) spec[f * L + a] = res[a];
+            __syncthreads();
+        }
+    }
+    // spectral products forming V1, Rx, Ry and S (df = 1) or Vgen (variable df)
+    for (int ka = threadIdx.x; ka < L; ka += blockDim.x) {
+        const KSpec<T> e = kspec[(size_t) kb * L + ka];
+        const C w1 = spec[ka], w2 = spec[L + ka], w3 = spec[2 * L + ka], w4 = spec[3 * L + ka];
+        // (i g) w = (-g w.y, g w.x)
+        const C gxw1 = mkc(-e.gx * w1.y, e.gx * w1.x);
+        const C gyw1 = mkc(-e.gy * w1.y, e.gy * w1.x);
+        const C v1 = cscale(w1, e.k);
+        const C rx = csub(gxw1, cscale(w2, e.k));
+        const C ry = csub(gyw1, cscale(w3, e.k));
+        C s4;
+        if (mode == KERNEL_DF1) {
+            const C gxw2 = mkc(-e.gx * w2.y, e.gx * w2.x);
+            const C gyw3 = mkc(-e.gy * w3.y, e.gy * w3.x);
+            s4 = cadd(csub(cscale(w1, e.h), cscale(cadd(gxw2, gyw3), T(2))), cscale(w4, e.k));
+        } else {
+            s4 = cscale(w1, e.h);
+        }
+        spec[ka] = v1;
+        spec[L + ka] = rx;
+        spec[2 * L + ka] = ry;
+        spec[3 * L + ka] = s4;
+    }
+    __syncthreads();
+    for (int f = 0; f < 4; ++f) {
+        C *res = fft_block(spec + f * L, scratch, 1, pl, tw, true);
+        for (int a = threadIdx.x; a < M; a += blockDim.x) d2[((size_t) f * M + a) * H + kb] = res[a];
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void k_data_rows_inv(const typename Cx<T>::t *__restrict__ d2, int M, FftPlan pl,
+                                const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out) {
+    typedef typename Cx<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = pl.L, H = L / 2 + 1;
+    C *bufa = reinterpret_cast<C *>(smem_raw);
+    C *bufb = bufa + 2 * L;
+    const int a = blockIdx.x;
+    for (int kb = threadIdx.x; kb < L; kb += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const C *rf = d2 + ((size_t) (2 * q) * M + a) * H;
+            const C *rg = d2 + ((size_t) (2 * q + 1) * M + a) * H;
+            C F, G;
+            if (kb < H) {
+                F = rf[kb];
+                G = rg[kb];
+            } else {
+                F = cconj(rf[L - kb]);
+                G = cconj(rg[L - kb]);
+            }
+            if (kb == 0 || 2 * kb == L) {
+                F.y = T(0);
+                G.y = T(0);
+            }
+            bufa[q * L + kb] = mkc(F.x - G.y, F.y + G.x);
+        }
+    }
+    __syncthreads();
+    C *res = fft_block(bufa, bufb, 2, pl, tw, true);
+    for (int b = threadIdx.x; b < M; b += blockDim.x) {
+        Cell4<T> v;
+        v.a = res[b].x;
+        v.b = res[b].y;
+        v.c = res[L + b].x;
+        v.d = res[L + b].y;
+        out[(size_t) a * M + b] = v;
+    }
+}
+
+// ---- 1-D ----
+template <typename T>
+__global__ void k_conv1d_fwd(const Cell4<T> *__restrict__ grid, int M, FftPlan pl,
+                             const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ work, T h,
+                             T df, int mode) {
+    typedef typename Cx<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = pl.L;
+    C *bufa = reinterpret_cast<C *>(smem_raw);
+    C *bufb = bufa + L;
+    const int f = blockIdx.x;  // 0..2 kernels (K, G, H|Kgen), 3..5 fields W1, W2', W3'
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        T v = 0;
+        if (f < 3) {
+            if (i < M || i > L - M) {
+                T k, g, hh;
+                kernel_vals_1d<T>(i < M ? i : i - L, h, df, mode, k, g, hh);
+                v = (f == 0) ? k : ((f == 1) ? g : hh);
+            }
+        } else if (i < M) {
+            const Cell4<T> c = grid[i];
+            v = (f == 3) ? c.a : ((f == 4) ? c.b : c.c);
+        }
+        bufa[i] = mkc(v, T(0));
+    }
+    __syncthreads();
+    C *res = fft_block(bufa, bufb, 1, pl, tw, false);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) work[(size_t) f * L + i] = res[i];
+}
+
+template <typename T>
+__global__ void k_conv1d_inv(const typename Cx<T>::t *__restrict__ work, int M, FftPlan pl,
+                             const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out, int mode) {
+    typedef typename Cx<T>::t C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int L = pl.L;
+    C *bufa = reinterpret_cast<C *>(smem_raw);
+    C *bufb = bufa + L;
+    const int o = blockIdx.x;
+    const T s = T(1) / T(L);
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        const T K = work[i].x * s;
+        const T G = work[L + i].y * s;
+        const T Hh = work[2 * L + i].x * s;
+        const C w1 = work[3 * L + i], w2 = work[4 * L + i], w3 = work[5 * L + i];
+        C v;
+        if (o == 0) {
+            v = cscale(w1, K);
+        } else if (o == 1) {
+            v = csub(mkc(-G * w1.y, G * w1.x), cscale(w2, K));
+        } else if (mode == KERNEL_DF1) {
+            v = cadd(csub(cscale(w1, Hh), cscale(mkc(-G * w2.y, G * w2.x), T(2))), cscale(w3, K));
+        } else {
+            v = cscale(w1, Hh);
+        }
+        bufa[i] = v;
+    }
+    __syncthreads();
+    C *res = fft_block(bufa, bufb, 1, pl, tw, true);
+    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+        T *cell = reinterpret_cast<T *>(out + i);
+        cell[o] = res[i].x;
+    }
+}
+
+template <typename K>
+cudaError_t set_smem(K kernel, size_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, const FftPlan &plan,
+                          const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
+                          KSpec<T> *kspec, double h, double df, int mode, cudaStream_t st) {
+    typedef typename Cx<T>::t C;
+    const int L = plan.L, H = L / 2 + 1;
+    if (L > max_fft_len<T>() || L < 2 * M) return cudaErrorInvalidValue;
+    const size_t s4 = 4 * (size_t) L * sizeof(C);
+    const size_t s5 = 5 * (size_t) L * sizeof(C);
+    cudaError_t e;
+    if ((e = set_smem(k_kernel_rows<T>, s4)) != cudaSuccess) return e;
+    if ((e = set_smem(k_kernel_cols<T>, s5)) != cudaSuccess) return e;
+    if ((e = set_smem(k_data_rows<T>, s4)) != cudaSuccess) return e;
+    if ((e = set_smem(k_data_cols<T>, s5)) != cudaSuccess) return e;
+    if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
+    const int thr = 256;
+    // kernel spectra: krow uses work_a ([4][L][H]); data passes use work_b ([4][M][H]) then work_a
+    k_kernel_rows<T><<<2 * M - 1, thr, s4, st>>>(M, plan, tw, work_a, (T) h, (T) df, mode);
+    k_kernel_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_a, kspec);
+    k_data_rows<T><<<M, thr, s4, st>>>(grid_in, M, plan, tw, work_b);
+    k_data_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_b, kspec, work_a, mode);
+    k_data_rows_inv<T><<<M, thr, s4, st>>>(work_a, M, plan, tw, grid_out);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t conv1d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, const FftPlan &plan,
+                          const typename Cx<T>::t *tw, typename Cx<T>::t *work, double h, double df, int mode,
+                          cudaStream_t st) {
+    typedef typename Cx<T>::t C;
+    const int L = plan.L;
+    const size_t s2 = 2 * (size_t) L * sizeof(C);
+    if (L < 2 * M || s2 > 227 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if ((e = set_smem(k_conv1d_fwd<T>, s2)) != cudaSuccess) return e;
+    if ((e = set_smem(k_conv1d_inv<T>, s2)) != cudaSuccess) return e;
+    k_conv1d_fwd<T><<<6, 512, s2, st>>>(grid_in, M, plan, tw, work, (T) h, (T) df, mode);
+    k_conv1d_inv<T><<<3, 512, s2, st>>>(work, M, plan, tw, grid_out, mode);
+    return cudaGetLastError();
+}
+
+template cudaError_t conv2d_launch<float>(const Cell4<float> *, Cell4<float> *, int, const FftPlan &, const float2 *,
+                                          float2 *, float2 *, KSpec<float> *, double, double, int, cudaStream_t);
+template cudaError_t conv2d_launch<double>(const Cell4<double> *, Cell4<double> *, int, const FftPlan &,
+                                           const double2 *, double2 *, double2 *, KSpec<double> *, double, double,
+                                           int, cudaStream_t);
+template cudaError_t conv1d_launch<float>(const Cell4<float> *, Cell4<float> *, int, const FftPlan &, const float2 *,
+                                          float2 *, double, double, int, cudaStream_t);
+template cudaError_t conv1d_launch<double>(const Cell4<double> *, Cell4<double> *, int, const FftPlan &,
+                                           const double2 *, double2 *, double, double, int, cudaStream_t);
+
+}  // namespace fitsne

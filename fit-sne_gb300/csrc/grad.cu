@@ -1,0 +1,738 @@
+// Per-point and per-edge kernels of one FIt-SNE gradient iteration (see grad.cuh).
+#include <cfloat>
+
+#include "grad.cuh"
+
+namespace fitsne {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kRedGrid = 1216;  // 152 SMs x 8 resident blocks of 256 threads
+constexpr int kAttrUnroll = 4;  // CSR edges per lane per batch in the attraction pass
+
+// ---------------------------------------------------------------------------------
+// storage layouts of Y
+template <typename T, int D>
+struct YL;
+template <>
+struct YL<float, 2> {
+    typedef df32 P;
+    static FITSNE_D void load(const float *Y, int i, P *c) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(Y) + i);
+        c[0] = {v.x, v.z};
+        c[1] = {v.y, v.w};
+    }
+    static FITSNE_D void store(float *Y, int i, const P *c) {
+        reinterpret_cast<float4 *>(Y)[i] = make_float4(c[0].hi, c[1].hi, c[0].lo, c[1].lo);
+    }
+};
+template <>
+struct YL<float, 1> {
+    typedef df32 P;
+    static FITSNE_D void load(const float *Y, int i, P *c) {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(Y) + i);
+        c[0] = {v.x, v.y};
+    }
+    static FITSNE_D void store(float *Y, int i, const P *c) {
+        reinterpret_cast<float2 *>(Y)[i] = make_float2(c[0].hi, c[0].lo);
+    }
+};
+template <>
+struct YL<double, 2> {
+    typedef double P;
+    static FITSNE_D void load(const double *Y, int i, P *c) {
+        const double2 v = __ldg(reinterpret_cast<const double2 *>(Y) + i);
+        c[0] = v.x;
+        c[1] = v.y;
+    }
+    static FITSNE_D void store(double *Y, int i, const P *c) {
+        reinterpret_cast<double2 *>(Y)[i] = make_double2(c[0], c[1]);
+    }
+};
+template <>
+struct YL<double, 1> {
+    typedef double P;
+    static FITSNE_D void load(const double *Y, int i, P *c) { c[0] = __ldg(Y + i); }
+    static FITSNE_D void store(double *Y, int i, const P *c) { Y[i] = c[0]; }
+};
+
+FITSNE_D float pdiff(df32 a, df32 b) { return df_diff(a, b); }
+FITSNE_D double pdiff(double a, double b) { return a - b; }
+FITSNE_D df32 padd(df32 a, float u) { return df_add_f(a, u); }
+FITSNE_D double padd(double a, double u) { return a + u; }
+FITSNE_D df32 pshift(df32 a, df32 negm) { return df_add(a, negm); }
+FITSNE_D double pshift(double a, double negm) { return a + negm; }
+FITSNE_D double ptod(df32 a) { return (double) a.hi + (double) a.lo; }
+FITSNE_D double ptod(double a) { return a; }
+
+// ---------------------------------------------------------------------------------
+// box geometry in the precision of T
+template <typename T>
+struct BoxP;
+template <>
+struct BoxP<float> {
+    df32 neg_mn, bw;
+    float inv_bw, bwT;
+    int nb, nterms, M;
+    float s[kMaxInterp], inv_den[kMaxInterp];
+};
+template <>
+struct BoxP<double> {
+    double mn, bw, bwT;
+    int nb, nterms, M;
+    double s[kMaxInterp], inv_den[kMaxInterp];
+};
+
+BoxP<float> make_box(const GridGeom &g, float *) {
+    BoxP<float> b;
+    b.neg_mn = df_from_double(-g.mn);
+    b.bw = df_from_double(g.bw);
+    b.inv_bw = (float) (1.0 / g.bw);
+    b.bwT = (float) g.bw;
+    b.nb = g.nb;
+    b.nterms = g.nterms;
+    b.M = g.M;
+    for (int k = 0; k < kMaxInterp; ++k) {
+        b.s[k] = g.s32[k];
+        b.inv_den[k] = g.inv_den32[k];
+    }
+    return b;
+}
+BoxP<double> make_box(const GridGeom &g, double *) {
+    BoxP<double> b;
+    b.mn = g.mn;
+    b.bw = g.bw;
+    b.bwT = g.bw;
+    b.nb = g.nb;
+    b.nterms = g.nterms;
+    b.M = g.M;
+    for (int k = 0; k < kMaxInterp; ++k) {
+        b.s[k] = g.s64[k];
+        b.inv_den[k] = g.inv_den64[k];
+    }
+    return b;
+}
+
+// box index (truncated and clamped as in n_body_fft_2d, nbodyfft.cpp:82-114) and the
+// in-box coordinate t = (x - lower) / width
+FITSNE_D void box_coord(df32 c, const BoxP<float> &b, int &k, float &t) {
+    const df32 d = df_add(c, b.neg_mn);
+    const float q = (d.hi + d.lo) * b.inv_bw;
+    k = (int) q;
+    if (k >= b.nb) k = b.nb - 1;
+    else if (k < 0) k = 0;
+    df32 p = two_prod((float) k, b.bw.hi);
+    p.lo += (float) k * b.bw.lo;
+    const df32 r = df_add(d, df_neg(p));
+    t = (r.hi + r.lo) * b.inv_bw;
+}
+FITSNE_D void box_coord(double c, const BoxP<double> &b, int &k, double &t) {
+    k = (int) ((c - b.mn) / b.bw);
+    if (k >= b.nb) k = b.nb - 1;
+    else if (k < 0) k = 0;
+    t = (c - (k * b.bw + b.mn)) / b.bw;
+}
+
+// Lagrange basis on the nodes s_k = (k + 1/2) / nterms (interpolate, nbodyfft.cpp:310-336)
+template <typename T, int NT>
+FITSNE_D void lagrange(T t, const BoxP<T> &b, T *w) {
+    const int n = NT > 0 ? NT : b.nterms;
+#pragma unroll
+    for (int j = 0; j < (NT > 0 ? NT : kMaxInterp); ++j) {
+        if (j < n) {
+            T num = T(1);
+#pragma unroll
+            for (int k = 0; k < (NT > 0 ? NT : kMaxInterp); ++k)
+                if (k < n && k != j) num *= (t - b.s[k]);
+            w[j] = num * b.inv_den[j];
+        }
+    }
+}
+
+FITSNE_D void atomic_add4(Cell4<float> *p, const Cell4<float> &v) {
+    atomicAdd(reinterpret_cast<float4 *>(p), make_float4(v.a, v.b, v.c, v.d));
+}
+FITSNE_D void atomic_add4(Cell4<double> *p, const Cell4<double> &v) {
+    atomicAdd(&p->a, v.a);
+    atomicAdd(&p->b, v.b);
+    atomicAdd(&p->c, v.c);
+    atomicAdd(&p->d, v.d);
+}
+
+// ---------------------------------------------------------------------------------
+// block reductions with a deterministic "last block finishes" step
+template <int NV>
+FITSNE_D void block_sum(double (&v)[NV], double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double x = v[k];
+        for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[wid * NV + k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double x = 0.0;
+            for (int w = 0; w < nw; ++w) x += sh[w * NV + k];
+            v[k] = x;
+        }
+    }
+    __syncthreads();
+}
+
+// Writes this block's partials; returns true in thread 0 of the last block to finish,
+// with v replaced by the total over all blocks (summed in block order).
+template <int NV>
+FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, double *sh) {
+    block_sum<NV>(v, sh);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = v[k];
+        __threadfence();
+        const unsigned int prev = atomicAdd(count, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (int b = threadIdx.x; b < (int) gridDim.x; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += ((volatile double *) part)[b * NV + k];
+    block_sum<NV>(acc, sh);
+    if (threadIdx.x == 0) {
+        *count = 0u;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = acc[k];
+        return true;
+    }
+    return false;
+}
+
+// min / max with the same rule as the reference
+template <int NV>
+FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *count, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) {
+        sh[2 * wid] = mn;
+        sh[2 * wid + 1] = mx;
+    }
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w) {
+            mn = fmin(mn, sh[2 * w]);
+            mx = fmax(mx, sh[2 * w + 1]);
+        }
+        part[2 * blockIdx.x] = mn;
+        part[2 * blockIdx.x + 1] = mx;
+        __threadfence();
+        const unsigned int prev = atomicAdd(count, 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double a = HUGE_VAL, b = -HUGE_VAL;
+    for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
+        a = fmin(a, ((volatile double *) part)[2 * k]);
+        b = fmax(b, ((volatile double *) part)[2 * k + 1]);
+    }
+    for (int o = 16; o; o >>= 1) {
+        a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    __syncthreads();
+    if (lane == 0) {
+        sh[2 * wid] = a;
+        sh[2 * wid + 1] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w) {
+            a = fmin(a, sh[2 * w]);
+            b = fmax(b, sh[2 * w + 1]);
+        }
+        mn = a;
+        mx = b;
+        *count = 0u;
+        return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------------
+// center (subtract the pending mean) + min/max (tsne.cpp:531, 1039-1049, 769-773)
+template <typename T, int D>
+__global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply_mean, RedScratch r) {
+    typedef typename YL<T, D>::P P;
+    __shared__ double sh[2 * 32];
+    P negm[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const double m = apply_mean ? r.mean[d] : 0.0;
+        if constexpr (sizeof(T) == 4)
+            negm[d] = df_from_double(-m);
+        else
+            negm[d] = -m;
+    }
+    double mn = HUGE_VAL, mx = -HUGE_VAL;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        P c[D];
+        YL<T, D>::load(Y, i, c);
+        if (apply_mean) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) c[d] = pshift(c[d], negm[d]);
+            YL<T, D>::store(Y, i, c);
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const double v = ptod(c[d]);
+            mx = fmax(mx, v);
+            // 2-D: the first coordinate of the first point never reaches the min
+            // (if / else-if pair of tsne.cpp:1045-1048)
+            if (!(D == 2 && i == 0 && d == 0)) mn = fmin(mn, v);
+        }
+    }
+    if (grid_minmax<2>(mn, mx, r.part, r.count + 0, sh)) {
+        r.mnmx[0] = mn;
+        r.mnmx[1] = mx;
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// spread (step 1 of n_body_fft_2d / nbodyfft) in box-local charges
+template <typename T, int D, int NT>
+__global__ void __launch_bounds__(kBlock) k_spread(const T *__restrict__ Y, int N, BoxP<T> b,
+                                                   Cell4<T> *__restrict__ grid) {
+    typedef typename YL<T, D>::P P;
+    const int n = NT > 0 ? NT : b.nterms;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        P c[D];
+        YL<T, D>::load(Y, i, c);
+        int bx[D];
+        T t[D];
+        T w[D][NT > 0 ? NT : kMaxInterp];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            box_coord(c[d], b, bx[d], t[d]);
+            lagrange<T, NT>(t[d], b, w[d]);
+        }
+        if constexpr (D == 2) {
+            for (int ia = 0; ia < n; ++ia) {
+                const T ux = (t[0] - b.s[ia]) * b.bwT;
+                const size_t rowbase = (size_t) (bx[0] * n + ia) * b.M + bx[1] * n;
+                for (int ib = 0; ib < n; ++ib) {
+                    const T uy = (t[1] - b.s[ib]) * b.bwT;
+                    const T ww = w[0][ia] * w[1][ib];
+                    Cell4<T> v;
+                    v.a = ww;
+                    v.b = ww * ux;
+                    v.c = ww * uy;
+                    v.d = ww * (ux * ux + uy * uy);
+                    atomic_add4(grid + rowbase + ib, v);
+                }
+            }
+        } else {
+            for (int ia = 0; ia < n; ++ia) {
+                const T u = (t[0] - b.s[ia]) * b.bwT;
+                const T ww = w[0][ia];
+                T *cell = reinterpret_cast<T *>(grid + bx[0] * n + ia);
+                atomicAdd(cell + 0, ww);
+                atomicAdd(cell + 1, ww * u);
+                atomicAdd(cell + 2, ww * u * u);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// gather (step 3) + the repulsion numerators + Z
+template <typename T, int D, int NT>
+__global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int N, BoxP<T> b,
+                                                   const Cell4<T> *__restrict__ pot, int mode,
+                                                   T *__restrict__ rep, RedScratch r) {
+    typedef typename YL<T, D>::P P;
+    __shared__ double sh[32];
+    const int n = NT > 0 ? NT : b.nterms;
+    double zacc[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        P c[D];
+        YL<T, D>::load(Y, i, c);
+        int bx[D];
+        T t[D];
+        T w[D][NT > 0 ? NT : kMaxInterp];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            box_coord(c[d], b, bx[d], t[d]);
+            lagrange<T, NT>(t[d], b, w[d]);
+        }
+        T zi = T(0);
+        if constexpr (D == 2) {
+            T rx = T(0), ry = T(0);
+            for (int ia = 0; ia < n; ++ia) {
+                const T ux = (t[0] - b.s[ia]) * b.bwT;
+                const size_t rowbase = (size_t) (bx[0] * n + ia) * b.M + bx[1] * n;
+                for (int ib = 0; ib < n; ++ib) {
+                    const T uy = (t[1] - b.s[ib]) * b.bwT;
+                    const T ww = w[0][ia] * w[1][ib];
+                    const Cell4<T> p = pot[rowbase + ib];
+                    rx += ww * (ux * p.a + p.b);
+                    ry += ww * (uy * p.a + p.c);
+                    if (mode == KERNEL_DF1)
+                        zi += ww * ((T(1) + ux * ux + uy * uy) * p.a + T(2) * (ux * p.b + uy * p.c) + p.d);
+                    else
+                        zi += ww * p.d;
+                }
+            }
+            rep[2 * (size_t) i] = rx;
+            rep[2 * (size_t) i + 1] = ry;
+        } else {
+            T rx = T(0);
+            for (int ia = 0; ia < n; ++ia) {
+                const T u = (t[0] - b.s[ia]) * b.bwT;
+                const Cell4<T> p = pot[bx[0] * n + ia];
+                rx += w[0][ia] * (u * p.a + p.b);
+                if (mode == KERNEL_DF1)
+                    zi += w[0][ia] * ((T(1) + u * u) * p.a + T(2) * u * p.b + p.c);
+                else
+                    zi += w[0][ia] * p.c;
+            }
+            rep[i] = rx;
+        }
+        zacc[0] += (double) zi;
+    }
+    if (grid_sum<1>(zacc, r.part, r.count + 1, sh)) *r.z = zacc[0] - (double) N;
+}
+
+// ---------------------------------------------------------------------------------
+// CSR attraction fused with the optimiser step (tsne.cpp:1121-1155 and 479-531).
+// One warp per row; rows are strided over a fixed grid so that the mean of the new Y
+// reduces over few partials.
+template <typename T, int D>
+__global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                                                 const T *__restrict__ val, const T *__restrict__ Yin,
+                                                 T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
+                                                 T *__restrict__ dC, const T *__restrict__ rep, int N,
+                                                 UpdateParams p, RedScratch r) {
+    typedef typename YL<T, D>::P P;
+    __shared__ double sh[2 * 32];
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const double Zd = *r.z;
+    const T zinv = T(1.0 / Zd);
+    const T df = T(p.df);
+    const bool df1 = (p.df == 1.0);
+    const T exag = T(p.exag);
+    P msum[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        if constexpr (sizeof(T) == 4)
+            msum[d] = {0.f, 0.f};
+        else
+            msum[d] = 0.0;
+    }
+    for (int i = gw; i < N; i += nw) {
+        P ci[D];
+        YL<T, D>::load(Yin, i, ci);
+        T a[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) a[d] = T(0);
+        const uint32_t e0 = row[i], e1 = row[i + 1];
+        // kAttrUnroll edges per lane per batch: all index / value loads first, then all
+        // neighbour gathers, so that each lane has several independent loads in flight
+        for (uint32_t base = e0; base < e1; base += 32 * kAttrUnroll) {
+            uint32_t j[kAttrUnroll];
+            T v[kAttrUnroll];
+#pragma unroll
+            for (int k = 0; k < kAttrUnroll; ++k) {
+                const uint32_t e = base + lane + 32 * k;
+                const bool ok = e < e1;
+                j[k] = ok ? __ldcs(col + e) : (uint32_t) i;
+                v[k] = ok ? __ldcs(val + e) : T(0);
+            }
+            P cj[kAttrUnroll][D];
+#pragma unroll
+            for (int k = 0; k < kAttrUnroll; ++k) YL<T, D>::load(Yin, (int) j[k], cj[k]);
+#pragma unroll
+            for (int k = 0; k < kAttrUnroll; ++k) {
+                T dx[D];
+                T d2 = T(0);
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    dx[d] = pdiff(ci[d], cj[k][d]);
+                    d2 += dx[d] * dx[d];
+                }
+                const T q = df1 ? T(1) / (T(1) + d2) : T(1) / (T(1) + d2 / df);
+                const T vq = v[k] * q;
+#pragma unroll
+                for (int d = 0; d < D; ++d) a[d] += vq * dx[d];
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            for (int o = 16; o; o >>= 1) a[d] += __shfl_xor_sync(0xffffffffu, a[d], o);
+        if (lane == 0) {
+            T g[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) g[d] = exag * a[d] - rep[(size_t) i * D + d] * zinv;
+            if (p.mode == 0) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) dC[(size_t) i * D + d] = g[d];
+            } else {
+                P cn[D];
+                if (p.use_gains) {
+                    T u[D];
+                    T nrm2 = T(0);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        T gn = gains[(size_t) i * D + d];
+                        const T uo = uY[(size_t) i * D + d];
+                        gn = (sgn(g[d]) != sgn(uo)) ? (gn + T(0.2)) : (gn * T(0.8));
+                        if (gn < T(0.01)) gn = T(0.01);
+                        gains[(size_t) i * D + d] = gn;
+                        u[d] = T(p.momentum) * uo - T(p.learning_rate) * gn * g[d];
+                        nrm2 += u[d] * u[d];
+                    }
+                    if (p.max_step_norm > 0) {
+                        const T step = sqrt(nrm2);
+                        if (step > T(p.max_step_norm)) {
+                            const T sc = T(p.max_step_norm) / step;
+#pragma unroll
+                            for (int d = 0; d < D; ++d) u[d] *= sc;
+                        }
+                    }
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        uY[(size_t) i * D + d] = u[d];
+                        cn[d] = padd(ci[d], u[d]);
+                    }
+                } else {
+#pragma unroll
+                    for (int d = 0; d < D; ++d) cn[d] = padd(ci[d], -g[d]);
+                }
+                YL<T, D>::store(Yout, i, cn);
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    if constexpr (sizeof(T) == 4)
+                        msum[d] = df_add(msum[d], cn[d]);
+                    else
+                        msum[d] += cn[d];
+                }
+            }
+        }
+    }
+    if (p.mode != 0) {
+        double m[2] = {0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < D; ++d) m[d] = ptod(msum[d]);
+        if (grid_sum<2>(m, r.part, r.count + 2, sh)) {
+            r.mean[0] = m[0] / (double) N;
+            r.mean[1] = m[1] / (double) N;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// KL divergence over the CSR edges (evaluateErrorFft, tsne.cpp:1329-1355)
+template <typename T, int D>
+__global__ void __launch_bounds__(kBlock) k_kl(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                                               const T *__restrict__ val, const T *__restrict__ Y, int N,
+                                               double exag, double dfd, RedScratch r) {
+    typedef typename YL<T, D>::P P;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const T zinv = T(1.0 / *r.z);
+    const T df = T(dfd);
+    const T ex = T(exag);
+    double acc[1] = {0.0};
+    for (int i = gw; i < N; i += nw) {
+        P ci[D];
+        YL<T, D>::load(Y, i, ci);
+        const uint32_t e1 = row[i + 1];
+        for (uint32_t e = row[i] + lane; e < e1; e += 32) {
+            P cj[D];
+            YL<T, D>::load(Y, (int) col[e], cj);
+            T d2 = T(0);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const T dx = pdiff(ci[d], cj[d]);
+                d2 += dx * dx;
+            }
+            const T base = T(1) / (T(1) + d2 / df);
+            const T Q = (dfd == 1.0 ? base : pow(base, df)) * zinv;
+            const T pv = val[e] * ex;
+            acc[0] += (double) (pv * log((pv + T(FLT_MIN)) / (Q + T(FLT_MIN))));
+        }
+    }
+    if (grid_sum<1>(acc, r.part, r.count + 3, sh)) *r.kl = acc[0];
+}
+
+// ---------------------------------------------------------------------------------
+template <typename T, int D>
+__global__ void k_y_from_double(const double *__restrict__ src, T *__restrict__ Y, int N) {
+    typedef typename YL<T, D>::P P;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        P c[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            if constexpr (sizeof(T) == 4)
+                c[d] = df_from_double(src[(size_t) i * D + d]);
+            else
+                c[d] = src[(size_t) i * D + d];
+        }
+        YL<T, D>::store(Y, i, c);
+    }
+}
+template <typename T, int D>
+__global__ void k_y_to_double(const T *__restrict__ Y, double *__restrict__ dst, int N) {
+    typedef typename YL<T, D>::P P;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        P c[D];
+        YL<T, D>::load(Y, i, c);
+#pragma unroll
+        for (int d = 0; d < D; ++d) dst[(size_t) i * D + d] = ptod(c[d]);
+    }
+}
+template <typename T>
+__global__ void k_cast(const double *__restrict__ src, T *__restrict__ dst, size_t n) {
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x)
+        dst[i] = (T) src[i];
+}
+
+inline int grid_for(long long n, int per_block, int cap) {
+    long long g = (n + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int) g;
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, RedScratch r, cudaStream_t st) {
+    const int g = grid_for(N, kBlock, kRedGrid);
+    if (D == 2)
+        k_center_minmax<T, 2><<<g, kBlock, 0, st>>>(Y, N, apply_mean, r);
+    else
+        k_center_minmax<T, 1><<<g, kBlock, 0, st>>>(Y, N, apply_mean, r);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &gg, Cell4<T> *grid, cudaStream_t st) {
+    const BoxP<T> b = make_box(gg, (T *) nullptr);
+    const int g = grid_for(N, kBlock, 1 << 20);
+    if (D == 2) {
+        if (gg.nterms == 3)
+            k_spread<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+        else
+            k_spread<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+    } else {
+        if (gg.nterms == 3)
+            k_spread<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+        else
+            k_spread<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &gg, const Cell4<T> *pot, int mode, T *rep,
+                          RedScratch r, cudaStream_t st) {
+    const BoxP<T> b = make_box(gg, (T *) nullptr);
+    const int g = grid_for(N, kBlock, kRedGrid);
+    if (D == 2) {
+        if (gg.nterms == 3)
+            k_gather<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
+        else
+            k_gather<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
+    } else {
+        if (gg.nterms == 3)
+            k_gather<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
+        else
+            k_gather<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
+                               T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
+                               RedScratch r, cudaStream_t st) {
+    const int g = grid_for((long long) N * 32, kBlock, kRedGrid);
+    if (D == 2)
+        k_attr<T, 2><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
+    else
+        k_attr<T, 1><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_kl(const uint32_t *row, const uint32_t *col, const T *val, const T *Y, int N, int D, double exag,
+                      double df, RedScratch r, cudaStream_t st) {
+    const int g = grid_for((long long) N * 32, kBlock, kRedGrid);
+    if (D == 2)
+        k_kl<T, 2><<<g, kBlock, 0, st>>>(row, col, val, Y, N, exag, df, r);
+    else
+        k_kl<T, 1><<<g, kBlock, 0, st>>>(row, col, val, Y, N, exag, df, r);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_y_from_double(const double *src, T *Y, int N, int D, cudaStream_t st) {
+    const int g = grid_for(N, kBlock, 4096);
+    if (D == 2)
+        k_y_from_double<T, 2><<<g, kBlock, 0, st>>>(src, Y, N);
+    else
+        k_y_from_double<T, 1><<<g, kBlock, 0, st>>>(src, Y, N);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_y_to_double(const T *Y, double *dst, int N, int D, cudaStream_t st) {
+    const int g = grid_for(N, kBlock, 4096);
+    if (D == 2)
+        k_y_to_double<T, 2><<<g, kBlock, 0, st>>>(Y, dst, N);
+    else
+        k_y_to_double<T, 1><<<g, kBlock, 0, st>>>(Y, dst, N);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_cast_from_double(const double *src, T *dst, size_t n, cudaStream_t st) {
+    const int g = grid_for((long long) n, kBlock, 8192);
+    k_cast<T><<<g, kBlock, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+#define FITSNE_INST(T)                                                                                           \
+    template cudaError_t launch_center_minmax<T>(T *, int, int, int, RedScratch, cudaStream_t);                 \
+    template cudaError_t launch_spread<T>(const T *, int, int, const GridGeom &, Cell4<T> *, cudaStream_t);     \
+    template cudaError_t launch_gather<T>(const T *, int, int, const GridGeom &, const Cell4<T> *, int, T *,     \
+                                          RedScratch, cudaStream_t);                                            \
+    template cudaError_t launch_attr_update<T>(const uint32_t *, const uint32_t *, const T *, const T *, T *,    \
+                                               T *, T *, T *, const T *, int, int, const UpdateParams &,         \
+                                               RedScratch, cudaStream_t);                                       \
+    template cudaError_t launch_kl<T>(const uint32_t *, const uint32_t *, const T *, const T *, int, int, double, \
+                                      double, RedScratch, cudaStream_t);                                        \
+    template cudaError_t launch_y_from_double<T>(const double *, T *, int, int, cudaStream_t);                  \
+    template cudaError_t launch_y_to_double<T>(const T *, double *, int, int, cudaStream_t);                    \
+    template cudaError_t launch_cast_from_double<T>(const double *, T *, size_t, cudaStream_t);
+FITSNE_INST(float)
+FITSNE_INST(double)
+#undef FITSNE_INST
+
+}  // namespace fitsne

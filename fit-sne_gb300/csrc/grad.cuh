@@ -1,0 +1,91 @@
+// Per-iteration gradient kernels of FIt-SNE (everything except the FFT convolution).
+//
+// Reference functions replaced (src/ paths of KlugerLab/FIt-SNE v1.2.1):
+//   computeFftGradient          tsne.cpp:1027-1169   (2-D, df = 1)
+//   computeFftGradientVariableDf tsne.cpp:860-1024   (2-D, df != 1)
+//   computeFftGradientOneD      tsne.cpp:758-856     (1-D, df = 1)
+//   computeFftGradientOneDVariableDf tsne.cpp:647-754 (1-D, df != 1)
+//   n_body_fft_2d / nbodyfft steps 1 and 3, interpolate  nbodyfft.cpp:73-248, 310-455
+//   TSNE::run update loop + zeroMean                      tsne.cpp:479-531, 1851-1876
+//   evaluateErrorFft                                       tsne.cpp:1329-1355
+//
+// Charges are spread in box-local coordinates.  The reference spreads the charges
+// (1, x, y, x^2 + y^2) and forms the repulsion as x_i phi_1 - phi_2, which cancels
+// catastrophically in FP32 far from the origin.  Here each node b receives
+// (w, w*(x_j - x_b), w*(y_j - y_b), w*|y_j - y_b|^2), and the convolution uses the
+// kernels K, Gx = K*dx, Gy = K*dy, H = K*|d|^2 so that
+//   rep_x(i) = sum_a L_a(y_i) [ (x_i - x_a) V1(a) + Rx(a) ]
+//   Z_i      = sum_a L_a(y_i) [ (1 + |y_i - y_a|^2) V1(a) + 2 (y_i - y_a).R(a) + S(a) ]
+// with V1 = K*W1, Rx = Gx*W1 - K*W2', Ry = Gy*W1 - K*W3',
+//      S = H*W1 - 2 (Gx*W2' + Gy*W3') + K*W4'.
+// This is an exact algebraic rewrite of the reference's interpolated sums (same nodes,
+// same Lagrange weights, same kernel samples), so the FP64 form agrees with the
+// reference to rounding, and the FP32 form keeps every quantity box-local.
+#pragma once
+
+#include "common.cuh"
+#include "fftconv.cuh"
+
+namespace fitsne {
+
+// Interpolation grid of one gradient evaluation.
+struct GridGeom {
+    int nb;         // boxes per dimension
+    int nterms;     // interpolation points per box
+    int M;          // nterms * nb
+    double mn;      // lower corner (both axes in 2-D)
+    double bw;      // box width
+    double hk;      // node spacing used for the kernel samples (box width / nterms)
+    float s32[kMaxInterp], inv_den32[kMaxInterp];
+    double s64[kMaxInterp], inv_den64[kMaxInterp];
+};
+
+// Reduction scratch shared by the kernels of one embedding (device memory).
+struct RedScratch {
+    double *part;          // per-block partials, up to kMaxRedBlocks * 4 doubles
+    unsigned int *count;   // completion counters (4 slots)
+    double *mnmx;          // [min, max]
+    double *z;             // Z (sum_Q)
+    double *mean;          // mean of Y per dimension (2 doubles), consumed by center
+    double *kl;            // KL sum
+};
+constexpr int kMaxRedBlocks = 4096;
+
+struct UpdateParams {
+    int mode;               // 0 = write dC only, 1 = optimiser step (reference update rule)
+    int use_gains;          // gains/momentum branch (else plain Y -= dY)
+    double exag;            // multiplier of P in the attraction
+    double momentum;
+    double learning_rate;
+    double max_step_norm;   // <= 0: no clipping
+    double df;
+};
+
+// --- launchers (T = float: double-float Y of width 2*D; T = double: plain Y) ---------
+template <typename T>
+cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, RedScratch r, cudaStream_t st);
+template <typename T>
+cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &g, Cell4<T> *grid, cudaStream_t st);
+template <typename T>
+cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &g, const Cell4<T> *pot, int mode, T *rep,
+                          RedScratch r, cudaStream_t st);
+template <typename T>
+cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
+                               T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
+                               RedScratch r, cudaStream_t st);
+template <typename T>
+cudaError_t launch_kl(const uint32_t *row, const uint32_t *col, const T *val, const T *Y, int N, int D, double exag,
+                      double df, RedScratch r, cudaStream_t st);
+// host <-> device Y conversion (double array N*D <-> storage layout)
+template <typename T>
+cudaError_t launch_y_from_double(const double *src, T *Y, int N, int D, cudaStream_t st);
+template <typename T>
+cudaError_t launch_y_to_double(const T *Y, double *dst, int N, int D, cudaStream_t st);
+template <typename T>
+cudaError_t launch_cast_from_double(const double *src, T *dst, size_t n, cudaStream_t st);
+
+// width (in T elements) of one point's storage
+template <typename T>
+constexpr int y_width(int D) { return sizeof(T) == 4 ? 2 * D : D; }
+
+}  // namespace fitsne

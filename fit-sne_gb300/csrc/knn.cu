@@ -1,0 +1,428 @@
+// Exact kNN: FP32 candidate scan + FP64 re-rank with verification (see knn.cuh).
+#include <cfloat>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "knn.cuh"
+
+namespace fitsne {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRefTile = 64;
+constexpr int kDChunk = 64;
+constexpr int kStride = kDChunk + 4;  // 17 float4 units per row: conflict-free 16-byte loads
+constexpr int kSlack = 16;
+
+__device__ __forceinline__ bool pair_gt(float a, uint32_t ia, float b, uint32_t ib) {
+    return a > b || (a == b && ia > ib);
+}
+__device__ __forceinline__ bool pair_gt(double a, uint32_t ia, double b, uint32_t ib) {
+    return a > b || (a == b && ia > ib);
+}
+
+// ascending bitonic sort of n (power of two) (key, index) pairs in shared memory by one warp
+template <typename KT>
+__device__ void warp_bitonic(KT *d, uint32_t *ix, int n) {
+    const int lane = threadIdx.x & 31;
+    for (int k = 2; k <= n; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < n; i += 32) {
+                const int p = i ^ j;
+                if (p > i) {
+                    const bool up = (i & k) == 0;
+                    const KT a = d[i], b = d[p];
+                    const uint32_t ia = ix[i], ib = ix[p];
+                    if (pair_gt(a, ia, b, ib) == up) {
+                        d[i] = b;
+                        d[p] = a;
+                        ix[i] = ib;
+                        ix[p] = ia;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+}
+
+// Candidate scan.  Block = QPC queries; all N points stream through shared memory in tiles
+// of 64; each query keeps up to CAP candidates (sorted and cut to C when the list fills).
+template <int QPC, int CAP>
+__global__ void __launch_bounds__(kThreads) k_knn_cand(const float *__restrict__ Xf, int N, int Dp, int C,
+                                                       const int *__restrict__ qlist, int nq,
+                                                       float *__restrict__ out_d, uint32_t *__restrict__ out_i) {
+    constexpr int QPW = QPC / 8;  // queries per warp
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *qs = reinterpret_cast<float *>(smem_raw);      // [QPC][kStride]
+    float *rs = qs + QPC * kStride;                        // [kRefTile][kStride]
+    float *dt = rs + kRefTile * kStride;                   // [QPC][kRefTile + 1]
+    float *cd = dt + QPC * (kRefTile + 1);                 // [QPC][CAP]
+    uint32_t *ci = reinterpret_cast<uint32_t *>(cd + QPC * CAP);  // [QPC][CAP]
+    __shared__ int cnt[QPC];
+    __shared__ float thr[QPC];
+    __shared__ int qid[QPC];
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid < QPC) {
+        const int slot = blockIdx.x * QPC + tid;
+        qid[tid] = slot < nq ? (qlist ? qlist[slot] : slot) : -1;
+        cnt[tid] = 0;
+        thr[tid] = FLT_MAX;
+    }
+    __syncthreads();
+    const int nchunk = (Dp + kDChunk - 1) / kDChunk;
+    const int qv = kDChunk / 4;  // float4 per chunk row
+
+    auto load_queries = [&](int c0) {
+        for (int e = tid; e < QPC * qv; e += kThreads) {
+            const int q = e / qv, v = e % qv;
+            const int dcol = c0 + 4 * v;
+            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (qid[q] >= 0 && dcol < Dp) x = *reinterpret_cast<const float4 *>(Xf + (size_t) qid[q] * Dp + dcol);
+            *reinterpret_cast<float4 *>(qs + q * kStride + 4 * v) = x;
+        }
+    };
+    if (nchunk == 1) load_queries(0);
+
+    for (int r0 = 0; r0 < N; r0 += kRefTile) {
+        float acc[QPW][2];
+#pragma unroll
+        for (int a = 0; a < QPW; ++a) acc[a][0] = acc[a][1] = 0.f;
+        for (int ch = 0; ch < nchunk; ++ch) {
+            const int c0 = ch * kDChunk;
+            if (nchunk > 1) load_queries(c0);
+            for (int e = tid; e < kRefTile * qv; e += kThreads) {
+                const int r = e / qv, v = e % qv;
+                const int dcol = c0 + 4 * v;
+                float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (r0 + r < N && dcol < Dp) x = *reinterpret_cast<const float4 *>(Xf + (size_t) (r0 + r) * Dp + dcol);
+                *reinterpret_cast<float4 *>(rs + r * kStride + 4 * v) = x;
+            }
+            __syncthreads();
+            const int nv = min(qv, (Dp - c0 + 3) / 4);
+            for (int v = 0; v < nv; ++v) {
+                const float4 r0v = *reinterpret_cast<const float4 *>(rs + (2 * lane) * kStride + 4 * v);
+                const float4 r1v = *reinterpret_cast<const float4 *>(rs + (2 * lane + 1) * kStride + 4 * v);
+#pragma unroll
+                for (int a = 0; a < QPW; ++a) {
+                    const float4 q = *reinterpret_cast<const float4 *>(qs + (w * QPW + a) * kStride + 4 * v);
+                    float t;
+                    t = q.x - r0v.x; acc[a][0] = fmaf(t, t, acc[a][0]);
+                    t = q.y - r0v.y; acc[a][0] = fmaf(t, t, acc[a][0]);
+                    t = q.z - r0v.z; acc[a][0] = fmaf(t, t, acc[a][0]);
+                    t = q.w - r0v.w; acc[a][0] = fmaf(t, t, acc[a][0]);
+                    t = q.x - r1v.x; acc[a][1] = fmaf(t, t, acc[a][1]);
+                    t = q.y - r1v.y; acc[a][1] = fmaf(t, t, acc[a][1]);
+                    t = q.z - r1v.z; acc[a][1] = fmaf(t, t, acc[a][1]);
+                    t = q.w - r1v.w; acc[a][1] = fmaf(t, t, acc[a][1]);
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int a = 0; a < QPW; ++a) {
+            const int q = w * QPW + a;
+            dt[q * (kRefTile + 1) + 2 * lane] = (r0 + 2 * lane < N) ? acc[a][0] : FLT_MAX;
+            dt[q * (kRefTile + 1) + 2 * lane + 1] = (r0 + 2 * lane + 1 < N) ? acc[a][1] : FLT_MAX;
+        }
+        __syncwarp();
+        // selection: the warp owns its QPW queries' lists
+        const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+        for (int a = 0; a < QPW; ++a) {
+            const int q = w * QPW + a;
+            if (qid[q] < 0) continue;
+            int n = cnt[q];
+            const float th = thr[q];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int r = lane + 32 * h;
+                const float d = dt[q * (kRefTile + 1) + r];
+                const bool pass = (r0 + r < N) && (d < th);
+                const unsigned m = __ballot_sync(0xffffffffu, pass);
+                if (pass) {
+                    const int pos = n + __popc(m & lt);
+                    cd[q * CAP + pos] = d;
+                    ci[q * CAP + pos] = (uint32_t) (r0 + r);
+                }
+                n += __popc(m);
+            }
+            __syncwarp();
+            if (n > CAP - kRefTile) {
+                for (int i = n + lane; i < CAP; i += 32) {
+                    cd[q * CAP + i] = FLT_MAX;
+                    ci[q * CAP + i] = 0xffffffffu;
+                }
+                __syncwarp();
+                warp_bitonic<float>(cd + q * CAP, ci + q * CAP, CAP);
+                if (n >= C) {
+                    n = C;
+                    if (lane == 0) thr[q] = cd[q * CAP + C - 1];
+                }
+            }
+            if (lane == 0) cnt[q] = n;
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+    // final sort and write-out of the C best
+#pragma unroll
+    for (int a = 0; a < QPW; ++a) {
+        const int q = w * QPW + a;
+        if (qid[q] < 0) continue;
+        const int n = cnt[q];
+        for (int i = n + lane; i < CAP; i += 32) {
+            cd[q * CAP + i] = FLT_MAX;
+            ci[q * CAP + i] = 0xffffffffu;
+        }
+        __syncwarp();
+        warp_bitonic<float>(cd + q * CAP, ci + q * CAP, CAP);
+        const size_t slot = (size_t) (blockIdx.x * QPC + q);
+        for (int i = lane; i < C; i += 32) {
+            out_d[slot * C + i] = cd[q * CAP + i];
+            out_i[slot * C + i] = ci[q * CAP + i];
+        }
+        __syncwarp();
+    }
+}
+
+// FP64 re-rank of the candidates of each query (one warp per query) + verification.
+template <int CP>
+__global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ Xd, int N, int D, int K, int C,
+                                                    const int *__restrict__ qlist, int nq,
+                                                    const float *__restrict__ cand_d,
+                                                    const uint32_t *__restrict__ cand_i,
+                                                    const double *__restrict__ norms, double maxnorm,
+                                                    uint32_t *__restrict__ idx, double *__restrict__ dist,
+                                                    int *__restrict__ flag) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double *ed = reinterpret_cast<double *>(smem_raw) + w * CP;
+    uint32_t *ei = reinterpret_cast<uint32_t *>(reinterpret_cast<double *>(smem_raw) + 4 * CP) + w * CP;
+    const int slot = blockIdx.x * 4 + w;
+    if (slot >= nq) return;
+    const int q = qlist ? qlist[slot] : slot;
+    const double *xq = Xd + (size_t) q * D;
+    for (int c = lane; c < CP; c += 32) {
+        double e = DBL_MAX;
+        uint32_t j = 0xffffffffu;
+        if (c < C) {
+            j = cand_i[(size_t) slot * C + c];
+            if (j != 0xffffffffu) {
+                const double *xj = Xd + (size_t) j * D;
+                double dd = 0.0;
+                for (int d = 0; d < D; ++d) {
+                    const double f = __dsub_rn(xq[d], xj[d]);
+                    dd = __dadd_rn(dd, __dmul_rn(f, f));
+                }
+                e = __dsqrt_rn(dd);
+            }
+        }
+        ed[c] = e;
+        ei[c] = j;
+    }
+    __syncwarp();
+    warp_bitonic<double>(ed, ei, CP);
+    for (int k = lane; k < K; k += 32) {
+        idx[(size_t) q * K + k] = ei[k];
+        dist[(size_t) q * K + k] = ed[k];
+    }
+    if (lane == 0) {
+        int ok = 1;
+        if (C < N) {
+            // every point outside the list has an FP32 squared distance >= the C-th one
+            const double sC = (double) cand_d[(size_t) slot * C + C - 1];
+            const double u = 5.9604644775390625e-08;  // 2^-24
+            const double eps = 1.5 * ((D + 4) * u * sC + 4.0 * u * sqrt(sC) * (norms[q] + maxnorm)) + 1e-30;
+            const double sK = ed[K - 1] * ed[K - 1];
+            ok = (sK < sC - eps) ? 1 : 0;
+        }
+        flag[slot] = ok ? 0 : 1;
+    }
+}
+
+__global__ void k_to_f32(const double *__restrict__ Xd, float *__restrict__ Xf, int N, int D, int Dp) {
+    const size_t n = (size_t) N * Dp;
+    for (size_t e = blockIdx.x * (size_t) blockDim.x + threadIdx.x; e < n; e += (size_t) gridDim.x * blockDim.x) {
+        const size_t i = e / Dp;
+        const int d = (int) (e % Dp);
+        Xf[e] = d < D ? (float) Xd[i * D + d] : 0.f;
+    }
+}
+
+__global__ void k_norms(const double *__restrict__ Xd, int N, int D, double *__restrict__ norms) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int d = 0; d < D; ++d) s += Xd[(size_t) i * D + d] * Xd[(size_t) i * D + d];
+        norms[i] = sqrt(s);
+    }
+}
+
+int cap_for(int C) {
+    int cap = 128;
+    while (cap < C + kRefTile) cap <<= 1;
+    return cap;
+}
+
+size_t cand_smem(int qpc, int cap) {
+    return sizeof(float) * ((size_t) qpc * kStride + kRefTile * kStride + qpc * (kRefTile + 1)) +
+           (sizeof(float) + sizeof(uint32_t)) * (size_t) qpc * cap;
+}
+
+template <int QPC, int CAP>
+cudaError_t launch_cand(const float *Xf, int N, int Dp, int C, const int *qlist, int nq, float *od, uint32_t *oi,
+                        cudaStream_t st) {
+    const size_t sm = cand_smem(QPC, CAP);
+    cudaError_t e = cudaFuncSetAttribute(k_knn_cand<QPC, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+    if (e != cudaSuccess) return e;
+    const int blocks = (nq + QPC - 1) / QPC;
+    k_knn_cand<QPC, CAP><<<blocks, kThreads, sm, st>>>(Xf, N, Dp, C, qlist, nq, od, oi);
+    return cudaGetLastError();
+}
+
+cudaError_t dispatch_cand(int cap, const float *Xf, int N, int Dp, int C, const int *qlist, int nq, float *od,
+                          uint32_t *oi, cudaStream_t st) {
+    switch (cap) {
+        case 128: return launch_cand<32, 128>(Xf, N, Dp, C, qlist, nq, od, oi, st);
+        case 256: return launch_cand<32, 256>(Xf, N, Dp, C, qlist, nq, od, oi, st);
+        case 512: return launch_cand<32, 512>(Xf, N, Dp, C, qlist, nq, od, oi, st);
+        case 1024: return launch_cand<8, 1024>(Xf, N, Dp, C, qlist, nq, od, oi, st);
+        case 2048: return launch_cand<8, 2048>(Xf, N, Dp, C, qlist, nq, od, oi, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int CP>
+cudaError_t launch_rerank(const double *Xd, int N, int D, int K, int C, const int *qlist, int nq, const float *cd,
+                          const uint32_t *ci, const double *norms, double maxnorm, uint32_t *idx, double *dist,
+                          int *flag, cudaStream_t st) {
+    const size_t sm = 4 * (size_t) CP * (sizeof(double) + sizeof(uint32_t));
+    cudaError_t e = cudaFuncSetAttribute(k_knn_rerank<CP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+    if (e != cudaSuccess) return e;
+    k_knn_rerank<CP><<<(nq + 3) / 4, 128, sm, st>>>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist,
+                                                     flag);
+    return cudaGetLastError();
+}
+
+cudaError_t dispatch_rerank(int cp, const double *Xd, int N, int D, int K, int C, const int *qlist, int nq,
+                            const float *cd, const uint32_t *ci, const double *norms, double maxnorm, uint32_t *idx,
+                            double *dist, int *flag, cudaStream_t st) {
+    switch (cp) {
+        case 128: return launch_rerank<128>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
+        case 256: return launch_rerank<256>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
+        case 512: return launch_rerank<512>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
+        case 1024: return launch_rerank<1024>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
+        case 2048: return launch_rerank<2048>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+int pow2_at_least(int n) {
+    int p = 128;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+}  // namespace
+
+int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist, cudaStream_t st, KnnStats *stats,
+              const char **err) {
+    static thread_local std::string msg;
+    auto fail = [&](const char *what, cudaError_t e) {
+        msg = std::string(what) + ": " + cudaGetErrorString(e);
+        if (err) *err = msg.c_str();
+        return -10;
+    };
+    if (K < 1 || K > N) {
+        msg = "K must be in [1, N]";
+        if (err) *err = msg.c_str();
+        return -3;
+    }
+    const int Dp = (D + 3) / 4 * 4;
+    int C = K + kSlack;
+    if (C > N) C = N;
+    int cap = cap_for(C);
+    if (cap > 2048) {
+        msg = "too many neighbours requested for the on-chip candidate lists (K <= 1968)";
+        if (err) *err = msg.c_str();
+        return -3;
+    }
+    float *Xf = nullptr, *cd = nullptr;
+    uint32_t *ci = nullptr;
+    double *norms = nullptr;
+    int *flag = nullptr, *qlist = nullptr;
+    cudaError_t e;
+#define KCK(x)                              \
+    do {                                    \
+        e = (x);                            \
+        if (e != cudaSuccess) {             \
+            cudaFree(Xf);                   \
+            cudaFree(cd);                   \
+            cudaFree(ci);                   \
+            cudaFree(norms);                \
+            cudaFree(flag);                 \
+            cudaFree(qlist);                \
+            return fail(#x, e);             \
+        }                                   \
+    } while (0)
+    KCK(cudaMalloc(&Xf, sizeof(float) * (size_t) N * Dp));
+    KCK(cudaMalloc(&norms, sizeof(double) * N));
+    KCK(cudaMalloc(&flag, sizeof(int) * N));
+    KCK(cudaMalloc(&qlist, sizeof(int) * N));
+    k_to_f32<<<4096, 256, 0, st>>>(Xd, Xf, N, D, Dp);
+    k_norms<<<(N + 255) / 256, 256, 0, st>>>(Xd, N, D, norms);
+    std::vector<double> hn(N);
+    KCK(cudaMemcpyAsync(hn.data(), norms, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    KCK(cudaStreamSynchronize(st));
+    double maxnorm = 0.0;
+    for (double v : hn) maxnorm = v > maxnorm ? v : maxnorm;
+
+    // first pass over all rows
+    KCK(cudaMalloc(&cd, sizeof(float) * (size_t) N * C));
+    KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) N * C));
+    KCK(dispatch_cand(cap, Xf, N, Dp, C, nullptr, N, cd, ci, st));
+    KCK(dispatch_rerank(pow2_at_least(C), Xd, N, D, K, C, nullptr, N, cd, ci, norms, maxnorm, idx, dist, flag, st));
+    std::vector<int> hf(N);
+    KCK(cudaMemcpyAsync(hf.data(), flag, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
+    KCK(cudaStreamSynchronize(st));
+    std::vector<int> bad;
+    for (int i = 0; i < N; ++i)
+        if (hf[i]) bad.push_back(i);
+    if (stats) stats->rows_rescanned = (int) bad.size();
+    // rescans of the unverified rows with longer lists
+    while (!bad.empty() && C < N && cap < 2048) {
+        C = C * 4 < N ? C * 4 : N;
+        if (cap_for(C) > 2048) C = 2048 - kRefTile < N ? 2048 - kRefTile : N;
+        cap = cap_for(C);
+        const int nq = (int) bad.size();
+        cudaFree(cd);
+        cudaFree(ci);
+        cd = nullptr;
+        ci = nullptr;
+        KCK(cudaMalloc(&cd, sizeof(float) * (size_t) nq * C));
+        KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) nq * C));
+        KCK(cudaMemcpyAsync(qlist, bad.data(), sizeof(int) * nq, cudaMemcpyHostToDevice, st));
+        KCK(dispatch_cand(cap, Xf, N, Dp, C, qlist, nq, cd, ci, st));
+        KCK(dispatch_rerank(pow2_at_least(C), Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag,
+                            st));
+        std::vector<int> f2(nq);
+        KCK(cudaMemcpyAsync(f2.data(), flag, sizeof(int) * nq, cudaMemcpyDeviceToHost, st));
+        KCK(cudaStreamSynchronize(st));
+        std::vector<int> still;
+        for (int k = 0; k < nq; ++k)
+            if (f2[k]) still.push_back(bad[k]);
+        bad.swap(still);
+    }
+    if (stats) stats->rows_unverified = (int) bad.size();
+#undef KCK
+    cudaFree(Xf);
+    cudaFree(cd);
+    cudaFree(ci);
+    cudaFree(norms);
+    cudaFree(flag);
+    cudaFree(qlist);
+    return 0;
+}
+
+}  // namespace fitsne

@@ -1,0 +1,393 @@
+// C ABI: TSNE::run replacement and the input-similarity entry points.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "../../include/fitsne_gb300.h"
+#include "affinity.cuh"
+#include "capi_internal.h"
+#include "embedding.cuh"
+#include "knn.cuh"
+
+namespace fitsne {
+namespace {
+
+bool verbose() {
+    const char *q = std::getenv("FITSNE_QUIET");
+    return !(q && std::atoi(q) != 0);
+}
+
+struct Stream {
+    cudaStream_t s = nullptr;
+    Stream() { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); }
+    ~Stream() {
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
+// Gaussian random number of TSNE::randn (src/tsne.cpp:1880-1890), drawn from libc rand()
+// so that a seeded initialisation matches the reference bit for bit.
+double randn_polar() {
+    double x, y, radius;
+    do {
+        x = 2 * (std::rand() / ((double) RAND_MAX + 1)) - 1;
+        y = 2 * (std::rand() / ((double) RAND_MAX + 1)) - 1;
+        radius = (x * x) + (y * y);
+    } while ((radius >= 1.0) || (radius == 0.0));
+    radius = std::sqrt(-2 * std::log(radius) / radius);
+    x *= radius;
+    return x;
+}
+
+// P_row.dat / P_col.dat / P_val.dat of src/tsne.cpp:236-281 and 333-366
+int load_p_files(int N, std::vector<uint32_t> &row, std::vector<uint32_t> &col, std::vector<double> &val) {
+    FILE *h = std::fopen("P_row.dat", "rb");
+    if (!h) return set_error(FITSNE_E_IO, "could not open P_row.dat");
+    row.assign(N + 1, 0);
+    size_t got = std::fread(row.data(), sizeof(uint32_t), N + 1, h);
+    std::fclose(h);
+    if (got != (size_t) N + 1) return set_error(FITSNE_E_IO, "P_row.dat is shorter than N + 1 entries");
+    const size_t nnz = row[N];
+    col.assign(nnz, 0);
+    val.assign(nnz, 0.0);
+    if (!(h = std::fopen("P_val.dat", "rb"))) return set_error(FITSNE_E_IO, "could not open P_val.dat");
+    got = std::fread(val.data(), sizeof(double), nnz, h);
+    std::fclose(h);
+    if (got != nnz) return set_error(FITSNE_E_IO, "P_val.dat is too short");
+    if (!(h = std::fopen("P_col.dat", "rb"))) return set_error(FITSNE_E_IO, "could not open P_col.dat");
+    got = std::fread(col.data(), sizeof(uint32_t), nnz, h);
+    std::fclose(h);
+    if (got != nnz) return set_error(FITSNE_E_IO, "P_col.dat is too short");
+    for (size_t e = 0; e < nnz; ++e)
+        if (col[e] >= (uint32_t) N) return set_error(FITSNE_E_IO, "P_col.dat has an index out of range");
+    return 0;
+}
+
+int save_p_files(int N, const std::vector<uint32_t> &row, const std::vector<uint32_t> &col,
+                 const std::vector<double> &val) {
+    FILE *h;
+    const size_t nnz = row[N];
+    if (!(h = std::fopen("P_val.dat", "w+b"))) return set_error(FITSNE_E_IO, "could not open P_val.dat");
+    std::fwrite(val.data(), sizeof(double), nnz, h);
+    std::fclose(h);
+    if (!(h = std::fopen("P_col.dat", "w+b"))) return set_error(FITSNE_E_IO, "could not open P_col.dat");
+    std::fwrite(col.data(), sizeof(uint32_t), nnz, h);
+    std::fclose(h);
+    if (!(h = std::fopen("P_row.dat", "w+b"))) return set_error(FITSNE_E_IO, "could not open P_row.dat");
+    std::fwrite(row.data(), sizeof(uint32_t), N + 1, h);
+    std::fclose(h);
+    return 0;
+}
+
+template <typename T>
+int optimise(const DevCSR &P, double *Y, int N, int no_dims, const GridParams &gp, const Schedule &s, double *costs,
+             cudaStream_t st, bool vb) {
+    Embedding<T> emb;
+    int rc = emb.init_device(N, no_dims, P.row, P.col, P.val, P.nnz, Y, gp, st);
+    if (!rc) rc = emb.run_schedule(s, 0, s.max_iter, costs, vb);
+    if (!rc) rc = emb.get_Y(Y);
+    if (rc) return set_error(rc == -13 ? FITSNE_E_GRID : FITSNE_E_CUDA, emb.error());
+    return 0;
+}
+
+}  // namespace
+}  // namespace fitsne
+
+using namespace fitsne;
+
+extern "C" {
+
+int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexity, double theta, int rand_seed,
+               int skip_random_init, int max_iter, int stop_lying_iter, int mom_switch_iter, double momentum,
+               double final_momentum, double learning_rate, int K, double sigma, int nbody_algorithm, int knn_algo,
+               double early_exag_coeff, double *costs, int no_momentum_during_exag, int start_late_exag_iter,
+               double late_exag_coeff, int n_trees, int search_k, int nterms, double intervals_per_integer,
+               int min_num_intervals, unsigned int nthreads, int load_affinities, int perplexity_list_length,
+               double *perplexity_list, double df, double max_step_norm) {
+    (void) n_trees;
+    (void) search_k;
+    (void) nthreads;
+    const bool vb = verbose();
+    if (!X || !Y || N < 2 || D < 1) return set_error(FITSNE_E_ARG, "invalid data arguments");
+    if (N - 1 < 3 * perplexity) return set_error(FITSNE_E_ARG, "Perplexity too large for the number of data points!");
+    if (theta == .0) return set_error(FITSNE_E_UNSUPPORTED, "exact t-SNE (theta = 0) is not part of this build");
+    if (nbody_algorithm != 2)
+        return set_error(FITSNE_E_UNSUPPORTED, "only the FFT-accelerated gradient (nbody_algorithm 2) is built");
+    if (knn_algo != 1 && knn_algo != 2) return set_error(FITSNE_E_ARG, "Invalid knn_algo param");
+    if (no_dims != 1 && no_dims != 2)
+        return set_error(FITSNE_E_ARG, "FFT interpolation scheme supports only 1 or 2 output dimensions");
+    if (nterms < 1 || nterms > kMaxInterp) return set_error(FITSNE_E_ARG, "n_interpolation_points must be in [1, 8]");
+    if (!(intervals_per_integer > 0) || min_num_intervals < 1)
+        return set_error(FITSNE_E_ARG, "invalid interpolation grid parameters");
+    if (!(df > 0)) return set_error(FITSNE_E_ARG, "df must be positive");
+    if (perplexity == 0 && (perplexity_list_length < 1 || !perplexity_list))
+        return set_error(FITSNE_E_ARG, "perplexity 0 needs a perplexity list");
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    if (max_iter < 0) max_iter = 0;
+    if (costs)
+        for (int i = 0; i < max_iter; ++i) costs[i] = 0.0;
+    Stream st;
+    std::string err;
+    DevCSR P;
+    if (load_affinities == 1) {
+        if (vb) std::printf("Loading approximate input similarities from files...\n");
+        std::vector<uint32_t> row, col;
+        std::vector<double> val;
+        rc = load_p_files(N, row, col, val);
+        if (rc) return rc;
+        if (csr_to_device(row.data(), col.data(), val.data(), N, &P, st.s, err))
+            return set_error(FITSNE_E_CUDA, err);
+    } else {
+        const bool normalize = perplexity > 0 || perplexity_list_length > 0;
+        double *Xd = nullptr;
+        if (prepare_X(X, N, D, normalize, &Xd, st.s, err)) return set_error(FITSNE_E_CUDA, err);
+        int K_use;
+        double sigma_use;
+        if (perplexity < 0) {
+            K_use = K;
+            sigma_use = sigma;
+        } else {
+            if (perplexity > 0) {
+                K_use = (int) (3 * perplexity);
+            } else {
+                K_use = (int) (3 * perplexity_list[0]);
+                for (int pp = 1; pp < perplexity_list_length; ++pp)
+                    if (3 * perplexity_list[pp] > K_use) K_use = (int) (3 * perplexity_list[pp]);
+            }
+            sigma_use = -1;
+        }
+        if (K_use < 1 || K_use + 1 > N) {
+            cudaFree(Xd);
+            return set_error(FITSNE_E_ARG, "number of neighbours must be in [1, N - 1]");
+        }
+        if (vb) {
+            if (knn_algo == 1) std::printf("Annoy kNN requested: this build computes the exact kNN on the GPU\n");
+            std::printf("Computing input similarities (exact kNN, K = %d) on the GPU...\n", K_use);
+        }
+        DevCSR P0;
+        int krs = 0;
+        rc = gaussian_perplexity_device(Xd, N, D, K_use, perplexity, sigma_use,
+                                        perplexity == 0 ? perplexity_list_length : 0, perplexity_list, &P0, st.s,
+                                        err, &krs);
+        cudaFree(Xd);
+        if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
+        rc = symmetrize_device(P0, &P, st.s, err);
+        free_csr(P0);
+        if (rc) return set_error(FITSNE_E_CUDA, err);
+        double sum = 0.0;
+        if (normalize_device(P, &sum, st.s, err)) {
+            free_csr(P);
+            return set_error(FITSNE_E_CUDA, err);
+        }
+    }
+    if (load_affinities == 2) {
+        if (vb) std::printf("Saving approximate input similarities to files...\n");
+        std::vector<uint32_t> row(N + 1), col(P.nnz);
+        std::vector<double> val(P.nnz);
+        if (csr_to_host(P, row.data(), col.data(), val.data(), st.s, err)) {
+            free_csr(P);
+            return set_error(FITSNE_E_CUDA, err);
+        }
+        rc = save_p_files(N, row, col, val);
+        if (rc) {
+            free_csr(P);
+            return rc;
+        }
+    }
+    if (!skip_random_init) {
+        std::srand(rand_seed >= 0 ? (unsigned int) rand_seed : (unsigned int) std::time(nullptr));
+        for (size_t i = 0; i < (size_t) N * no_dims; ++i) Y[i] = randn_polar() * .0001;
+    }
+    if (early_exag_coeff == 0) {
+        double mx = 0.0;
+        if (max_row_sum_device(P, &mx, st.s, err)) {
+            free_csr(P);
+            return set_error(FITSNE_E_CUDA, err);
+        }
+        early_exag_coeff = 1.0 / (learning_rate * mx);
+    }
+    if (vb)
+        std::printf("Input similarities computed (nnz = %zu); learning embedding (FP%d form)...\n", P.nnz,
+                    precision_bits());
+    GridParams gp;
+    gp.nterms = nterms;
+    gp.intervals_per_integer = intervals_per_integer;
+    gp.min_num_intervals = min_num_intervals;
+    gp.df = df;
+    Schedule s;
+    s.max_iter = max_iter;
+    s.stop_lying_iter = stop_lying_iter;
+    s.mom_switch_iter = mom_switch_iter;
+    s.momentum = momentum;
+    s.final_momentum = final_momentum;
+    s.learning_rate = learning_rate;
+    s.early_exag_coeff = early_exag_coeff;
+    s.no_momentum_during_exag = no_momentum_during_exag;
+    s.start_late_exag_iter = start_late_exag_iter;
+    s.late_exag_coeff = late_exag_coeff;
+    s.max_step_norm = max_step_norm;
+    std::vector<double> costs_local;
+    if (!costs) {
+        costs_local.assign(max_iter > 0 ? max_iter : 1, 0.0);
+        costs = costs_local.data();
+    }
+    if (precision_bits() == 64)
+        rc = optimise<double>(P, Y, N, no_dims, gp, s, costs, st.s, vb);
+    else
+        rc = optimise<float>(P, Y, N, no_dims, gp, s, costs, st.s, vb);
+    free_csr(P);
+    return rc;
+}
+
+int fitsne_knn(const double *X, int N, int D, int K, unsigned int *indices, double *distances) {
+    if (!X || !indices || !distances || N < 1 || D < 1) return set_error(FITSNE_E_ARG, "invalid arguments");
+    if (K < 1 || K > N) return set_error(FITSNE_E_ARG, "K must be in [1, N]");
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    Stream st;
+    double *Xd = nullptr, *dist = nullptr;
+    uint32_t *idx = nullptr;
+    const char *kerr = nullptr;
+    cudaError_t e = cudaMalloc(&Xd, sizeof(double) * (size_t) N * D);
+    if (e == cudaSuccess) e = cudaMalloc(&idx, sizeof(uint32_t) * (size_t) N * K);
+    if (e == cudaSuccess) e = cudaMalloc(&dist, sizeof(double) * (size_t) N * K);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Xd, X, sizeof(double) * (size_t) N * D, cudaMemcpyHostToDevice, st.s);
+    if (e == cudaSuccess) {
+        rc = knn_exact(Xd, N, D, K, idx, dist, st.s, nullptr, &kerr);
+        if (!rc) {
+            e = cudaMemcpyAsync(indices, idx, sizeof(uint32_t) * (size_t) N * K, cudaMemcpyDeviceToHost, st.s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(distances, dist, sizeof(double) * (size_t) N * K, cudaMemcpyDeviceToHost, st.s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st.s);
+        }
+    }
+    cudaFree(Xd);
+    cudaFree(idx);
+    cudaFree(dist);
+    if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, kerr ? kerr : "kNN failed");
+    if (e != cudaSuccess) return set_error(FITSNE_E_CUDA, cudaGetErrorString(e));
+    return 0;
+}
+
+int fitsne_distances2similarities(const double *Dm, double *P, int nrows, int K, double perplexity, double sigma,
+                                  int perplexity_list_length, const double *perplexity_list, double *betas) {
+    if (!Dm || !P || nrows < 0 || K < 1) return set_error(FITSNE_E_ARG, "invalid arguments");
+    if (perplexity == 0 && (perplexity_list_length < 1 || !perplexity_list))
+        return set_error(FITSNE_E_ARG, "perplexity 0 needs a perplexity list");
+    if (nrows == 0) return 0;
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    Stream st;
+    std::string err;
+    double *d = nullptr, *p = nullptr, *b = nullptr;
+    const size_t n = (size_t) nrows * K;
+    cudaError_t e = cudaMalloc(&d, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&p, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&b, sizeof(double) * nrows);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, Dm, sizeof(double) * n, cudaMemcpyHostToDevice, st.s);
+    if (e == cudaSuccess) {
+        rc = calibrate_rows(d, K, 0, p, nrows, K, perplexity, sigma, perplexity == 0 ? perplexity_list_length : 0,
+                            perplexity_list, b, st.s, err);
+        if (!rc) {
+            e = cudaMemcpyAsync(P, p, sizeof(double) * n, cudaMemcpyDeviceToHost, st.s);
+            if (e == cudaSuccess && betas)
+                e = cudaMemcpyAsync(betas, b, sizeof(double) * nrows, cudaMemcpyDeviceToHost, st.s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st.s);
+        }
+    }
+    cudaFree(d);
+    cudaFree(p);
+    cudaFree(b);
+    if (rc) return set_error(FITSNE_E_CUDA, err);
+    if (e != cudaSuccess) return set_error(FITSNE_E_CUDA, cudaGetErrorString(e));
+    return 0;
+}
+
+static int to_malloced(const DevCSR &P, unsigned int **row_P, unsigned int **col_P, double **val_P, cudaStream_t st,
+                       std::string &err) {
+    unsigned int *r = (unsigned int *) std::malloc(sizeof(unsigned int) * (P.N + 1));
+    unsigned int *c = (unsigned int *) std::malloc(sizeof(unsigned int) * (P.nnz ? P.nnz : 1));
+    double *v = (double *) std::malloc(sizeof(double) * (P.nnz ? P.nnz : 1));
+    if (!r || !c || !v) {
+        std::free(r);
+        std::free(c);
+        std::free(v);
+        return set_error(FITSNE_E_NOMEM, "host allocation failed");
+    }
+    if (csr_to_host(P, r, c, v, st, err)) {
+        std::free(r);
+        std::free(c);
+        std::free(v);
+        return set_error(FITSNE_E_CUDA, err);
+    }
+    *row_P = r;
+    *col_P = c;
+    *val_P = v;
+    return 0;
+}
+
+int fitsne_gaussian_perplexity(const double *X, int N, int D, unsigned int **row_P, unsigned int **col_P,
+                               double **val_P, double perplexity, int K, double sigma, unsigned int nthreads,
+                               int perplexity_list_length, const double *perplexity_list) {
+    (void) nthreads;
+    if (!X || !row_P || !col_P || !val_P || N < 2 || D < 1) return set_error(FITSNE_E_ARG, "invalid arguments");
+    if (K < 1 || K + 1 > N) return set_error(FITSNE_E_ARG, "K + 1 must not exceed N");
+    if (perplexity == 0 && (perplexity_list_length < 1 || !perplexity_list))
+        return set_error(FITSNE_E_ARG, "perplexity 0 needs a perplexity list");
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    Stream st;
+    std::string err;
+    double *Xd = nullptr;
+    cudaError_t e = cudaMalloc(&Xd, sizeof(double) * (size_t) N * D);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Xd, X, sizeof(double) * (size_t) N * D, cudaMemcpyHostToDevice, st.s);
+    if (e != cudaSuccess) {
+        cudaFree(Xd);
+        return set_error(FITSNE_E_CUDA, cudaGetErrorString(e));
+    }
+    DevCSR P;
+    rc = gaussian_perplexity_device(Xd, N, D, K, perplexity, sigma, perplexity == 0 ? perplexity_list_length : 0,
+                                    perplexity_list, &P, st.s, err);
+    cudaFree(Xd);
+    if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
+    rc = to_malloced(P, row_P, col_P, val_P, st.s, err);
+    free_csr(P);
+    return rc;
+}
+
+int fitsne_symmetrize(unsigned int **row_P, unsigned int **col_P, double **val_P, int N) {
+    if (!row_P || !col_P || !val_P || !*row_P || N < 1) return set_error(FITSNE_E_ARG, "invalid arguments");
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    const unsigned int *row = *row_P;
+    for (int n = 0; n < N; ++n)
+        if (row[n + 1] < row[n]) return set_error(FITSNE_E_ARG, "row pointers must be non-decreasing");
+    for (size_t e = 0; e < row[N]; ++e)
+        if ((*col_P)[e] >= (unsigned int) N) return set_error(FITSNE_E_ARG, "column index out of range");
+    Stream st;
+    std::string err;
+    DevCSR in, out;
+    if (csr_to_device(*row_P, *col_P, *val_P, N, &in, st.s, err)) return set_error(FITSNE_E_CUDA, err);
+    rc = symmetrize_device(in, &out, st.s, err);
+    free_csr(in);
+    if (rc) return set_error(FITSNE_E_CUDA, err);
+    unsigned int *r, *c;
+    double *v;
+    rc = to_malloced(out, &r, &c, &v, st.s, err);
+    free_csr(out);
+    if (rc) return rc;
+    std::free(*row_P);
+    std::free(*col_P);
+    std::free(*val_P);
+    *row_P = r;
+    *col_P = c;
+    *val_P = v;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,297 @@
+"""Python binding of the GB300 FIt-SNE library (ctypes over ``include/fitsne_gb300.h``).
+
+Every function here calls the in-tree ``libfitsne_gb300.so``; there is no CPU fallback:
+if the library is missing or no GPU is present the call raises :class:`FitsneError`.
+Names and argument meanings follow the reference's C++ interface (``TSNE::run``,
+``computeFftGradient`` ...); see the C header for the citation of each entry point.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfitsne_gb300.so")
+BIN_PATH = os.path.join(HERE, "bin", "fast_tsne")
+
+_u32p = ctypes.POINTER(ctypes.c_uint)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int)
+_lib = None
+
+# exported symbols and their signatures (restype, argtypes)
+_SIGS = {
+    "fitsne_run": (ctypes.c_int, [_f64p, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                  ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double, _f64p,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint, ctypes.c_int,
+                                  ctypes.c_int, _f64p, ctypes.c_double, ctypes.c_double]),
+    "fitsne_fft_gradient": (ctypes.c_int, [_u32p, _u32p, _f64p, _f64p, ctypes.c_int, ctypes.c_int, _f64p,
+                                           ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, _f64p]),
+    "fitsne_evaluate_error_fft": (ctypes.c_int, [_u32p, _u32p, _f64p, _f64p, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_double, ctypes.c_double, _f64p]),
+    "fitsne_knn": (ctypes.c_int, [_f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u32p, _f64p]),
+    "fitsne_distances2similarities": (ctypes.c_int, [_f64p, _f64p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                     ctypes.c_double, ctypes.c_int, _f64p, _f64p]),
+    "fitsne_gaussian_perplexity": (ctypes.c_int, [_f64p, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.POINTER(_u32p), ctypes.POINTER(_u32p),
+                                                  ctypes.POINTER(_f64p), ctypes.c_double, ctypes.c_int,
+                                                  ctypes.c_double, ctypes.c_uint, ctypes.c_int, _f64p]),
+    "fitsne_symmetrize": (ctypes.c_int, [ctypes.POINTER(_u32p), ctypes.POINTER(_u32p), ctypes.POINTER(_f64p),
+                                         ctypes.c_int]),
+    "fitsne_load_data": (ctypes.c_int, [ctypes.c_char_p] + [ctypes.c_void_p] * 32),
+    "fitsne_save_data": (ctypes.c_int, [ctypes.c_char_p, _f64p, _f64p, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int]),
+    "fitsne_session_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, _u32p,
+                                             _u32p, _f64p, _f64p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_int]),
+    "fitsne_session_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_double, _f64p]),
+    "fitsne_session_get_y": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
+    "fitsne_session_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fitsne_session_stage_times": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
+    "fitsne_session_destroy": (None, [ctypes.c_void_p]),
+    "fitsne_set_precision": (None, [ctypes.c_int]),
+    "fitsne_get_precision": (ctypes.c_int, []),
+    "fitsne_last_error": (ctypes.c_char_p, []),
+    "fitsne_version": (ctypes.c_char_p, []),
+    "fitsne_free": (None, [ctypes.c_void_p]),
+}
+
+
+class FitsneError(RuntimeError):
+    """Raised when the native library is missing or a call fails."""
+
+
+def lib() -> ctypes.CDLL:
+    """Loads the in-tree library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FitsneError("libfitsne_gb300.so not built: run fit-sne_gb300/build.py")
+        l = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(l, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    """Names declared by the C header (those this binding knows)."""
+    return list(_SIGS)
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        msg = lib().fitsne_last_error()
+        raise FitsneError("fitsne error %d: %s" % (rc, msg.decode() if msg else ""))
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def _csr(row_P, col_P, val_P):
+    row = np.ascontiguousarray(row_P, dtype=np.uint32)
+    col = np.ascontiguousarray(col_P, dtype=np.uint32)
+    val = np.ascontiguousarray(val_P, dtype=np.float64)
+    if len(col) == 0:
+        col = np.zeros(1, np.uint32)
+        val = np.zeros(1, np.float64)
+    return row, col, val
+
+
+def set_precision(bits: int) -> None:
+    """32 (default FP32 form) or 64 (plain FP64 form) for the one-shot entry points."""
+    lib().fitsne_set_precision(int(bits))
+
+
+def get_precision() -> int:
+    return int(lib().fitsne_get_precision())
+
+
+def fft_gradient(row_P, col_P, val_P, Y, nterms=3, intervals_per_integer=1.0, min_num_intervals=50, df=1.0):
+    """One FFT-interpolation gradient (computeFftGradient* of the reference).
+
+    Returns ``(dC, sum_Q)`` with dC of Y's shape (N x no_dims)."""
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    if Y.ndim == 1:
+        Y = Y[:, None]
+    N, d = Y.shape
+    row, col, val = _csr(row_P, col_P, val_P)
+    dC = np.zeros((N, d))
+    z = ctypes.c_double(0.0)
+    _check(lib().fitsne_fft_gradient(_p(row, _u32p), _p(col, _u32p), _p(val, _f64p), _p(Y, _f64p), N, d,
+                                     _p(dC, _f64p), int(nterms), float(intervals_per_integer),
+                                     int(min_num_intervals), float(df), ctypes.byref(z)))
+    return dC, z.value
+
+
+def evaluate_error_fft(row_P, col_P, val_P, Y, df, sum_Q) -> float:
+    """KL over the edges with a given Z (evaluateErrorFft of the reference)."""
+    Y = np.ascontiguousarray(Y, dtype=np.float64)
+    if Y.ndim == 1:
+        Y = Y[:, None]
+    N, d = Y.shape
+    row, col, val = _csr(row_P, col_P, val_P)
+    c = ctypes.c_double(0.0)
+    _check(lib().fitsne_evaluate_error_fft(_p(row, _u32p), _p(col, _u32p), _p(val, _f64p), _p(Y, _f64p), N, d,
+                                           float(df), float(sum_Q), ctypes.byref(c)))
+    return c.value
+
+
+def knn(X, K):
+    """Exact K nearest neighbours, self included: ``(indices[N,K] u32, distances[N,K])``."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    N, D = X.shape
+    idx = np.zeros((N, K), np.uint32)
+    dist = np.zeros((N, K))
+    _check(lib().fitsne_knn(_p(X, _f64p), N, D, int(K), _p(idx, _u32p), _p(dist, _f64p)))
+    return idx, dist
+
+
+def distances2similarities(Dist, perplexity, sigma=-1.0, perplexity_list=None):
+    """Row-wise calibration of K neighbour distances: ``(P[nrows,K], betas[nrows])``."""
+    Dist = np.ascontiguousarray(Dist, dtype=np.float64)
+    nrows, K = Dist.shape
+    P = np.zeros_like(Dist)
+    betas = np.zeros(nrows)
+    pl = np.ascontiguousarray(perplexity_list if perplexity_list is not None else [0.0], dtype=np.float64)
+    npl = 0 if perplexity_list is None else len(perplexity_list)
+    _check(lib().fitsne_distances2similarities(_p(Dist, _f64p), _p(P, _f64p), nrows, K, float(perplexity),
+                                               float(sigma), npl, _p(pl, _f64p), _p(betas, _f64p)))
+    return P, betas
+
+
+def _take_malloced(ptr, n, ctype, dtype):
+    arr = np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True) if n else np.zeros(0, dtype)
+    lib().fitsne_free(ctypes.cast(ptr, ctypes.c_void_p))
+    return arr
+
+
+def gaussian_perplexity(X, perplexity, K, sigma=-1.0, perplexity_list=None):
+    """kNN + calibration (computeGaussianPerplexity, VP-tree overload): CSR (row, col, val)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    N, D = X.shape
+    r, c, v = _u32p(), _u32p(), _f64p()
+    pl = np.ascontiguousarray(perplexity_list if perplexity_list is not None else [0.0], dtype=np.float64)
+    npl = 0 if perplexity_list is None else len(perplexity_list)
+    _check(lib().fitsne_gaussian_perplexity(_p(X, _f64p), N, D, ctypes.byref(r), ctypes.byref(c),
+                                            ctypes.byref(v), float(perplexity), int(K), float(sigma), 0, npl,
+                                            _p(pl, _f64p)))
+    row = _take_malloced(r, N + 1, ctypes.c_uint, np.uint32)
+    nnz = int(row[-1])
+    return row, _take_malloced(c, nnz, ctypes.c_uint, np.uint32), _take_malloced(v, nnz, ctypes.c_double,
+                                                                                   np.float64)
+
+
+def _malloc_copy(a, ctype):
+    libc = ctypes.CDLL(None)
+    libc.malloc.restype = ctypes.c_void_p
+    libc.malloc.argtypes = [ctypes.c_size_t]
+    n = max(1, a.nbytes)
+    p = libc.malloc(n)
+    if not p:
+        raise MemoryError
+    ctypes.memmove(p, a.ctypes.data, a.nbytes)
+    return ctypes.cast(p, ctypes.POINTER(ctype))
+
+
+def symmetrize(row_P, col_P, val_P, N):
+    """(P + P^T)/2 on the union pattern (symmetrizeMatrix): returns the new CSR."""
+    row, col, val = _csr(row_P, col_P, val_P)
+    r = _malloc_copy(row, ctypes.c_uint)
+    c = _malloc_copy(col, ctypes.c_uint)
+    v = _malloc_copy(val, ctypes.c_double)
+    rc = lib().fitsne_symmetrize(ctypes.byref(r), ctypes.byref(c), ctypes.byref(v), int(N))
+    _check(rc)
+    row2 = _take_malloced(r, N + 1, ctypes.c_uint, np.uint32)
+    nnz = int(row2[-1])
+    return row2, _take_malloced(c, nnz, ctypes.c_uint, np.uint32), _take_malloced(v, nnz, ctypes.c_double,
+                                                                                   np.float64)
+
+
+def run(X, no_dims=2, perplexity=30.0, theta=0.5, rand_seed=-1, Y0=None, max_iter=1000, stop_lying_iter=250,
+        mom_switch_iter=250, momentum=0.5, final_momentum=0.8, learning_rate=200.0, K=-1, sigma=-1.0,
+        nbody_algorithm=2, knn_algo=2, early_exag_coeff=12.0, no_momentum_during_exag=False,
+        start_late_exag_iter=-1, late_exag_coeff=-1.0, n_trees=50, search_k=-1, nterms=3,
+        intervals_per_integer=1.0, min_num_intervals=50, nthreads=0, load_affinities=0, perplexity_list=None,
+        df=1.0, max_step_norm=5.0):
+    """TSNE::run with the reference's argument meaning; returns ``(Y, costs)``."""
+    X = np.ascontiguousarray(X, dtype=np.float64).copy()
+    N, D = X.shape
+    Y = np.zeros((N, no_dims)) if Y0 is None else np.ascontiguousarray(Y0, dtype=np.float64).reshape(N, no_dims).copy()
+    costs = np.zeros(max_iter)
+    pl = np.ascontiguousarray(perplexity_list if perplexity_list is not None else [0.0], dtype=np.float64)
+    npl = 0 if perplexity_list is None else len(perplexity_list)
+    _check(lib().fitsne_run(_p(X, _f64p), N, D, _p(Y, _f64p), int(no_dims), float(perplexity), float(theta),
+                            int(rand_seed), 0 if Y0 is None else 1, int(max_iter), int(stop_lying_iter),
+                            int(mom_switch_iter), float(momentum), float(final_momentum), float(learning_rate),
+                            int(K), float(sigma), int(nbody_algorithm), int(knn_algo), float(early_exag_coeff),
+                            _p(costs, _f64p), int(bool(no_momentum_during_exag)), int(start_late_exag_iter),
+                            float(late_exag_coeff), int(n_trees), int(search_k), int(nterms),
+                            float(intervals_per_integer), int(min_num_intervals), int(nthreads),
+                            int(load_affinities), npl, _p(pl, _f64p), float(df), float(max_step_norm)))
+    return Y, costs
+
+
+class Session:
+    """Device-resident optimisation of one embedding (P and Y stay on the GPU)."""
+
+    def __init__(self, row_P, col_P, val_P, Y0, nterms=3, intervals_per_integer=1.0, min_num_intervals=50,
+                 df=1.0, precision=32):
+        Y0 = np.ascontiguousarray(Y0, dtype=np.float64)
+        if Y0.ndim == 1:
+            Y0 = Y0[:, None]
+        self.N, self.no_dims = Y0.shape
+        self._row, self._col, self._val = _csr(row_P, col_P, val_P)
+        h = ctypes.c_void_p()
+        _check(lib().fitsne_session_create(ctypes.byref(h), self.N, self.no_dims, _p(self._row, _u32p),
+                                           _p(self._col, _u32p), _p(self._val, _f64p), _p(Y0, _f64p), int(nterms),
+                                           float(intervals_per_integer), int(min_num_intervals), float(df),
+                                           int(precision)))
+        self._h = h
+
+    def run(self, it0, it1, max_iter=1000, stop_lying_iter=250, mom_switch_iter=250, momentum=0.5,
+            final_momentum=0.8, learning_rate=200.0, early_exag_coeff=12.0, no_momentum_during_exag=False,
+            start_late_exag_iter=-1, late_exag_coeff=-1.0, max_step_norm=5.0, costs=None):
+        cp = _p(costs, _f64p) if costs is not None else None
+        _check(lib().fitsne_session_run(self._h, int(it0), int(it1), int(max_iter), int(stop_lying_iter),
+                                        int(mom_switch_iter), float(momentum), float(final_momentum),
+                                        float(learning_rate), float(early_exag_coeff),
+                                        int(bool(no_momentum_during_exag)), int(start_late_exag_iter),
+                                        float(late_exag_coeff), float(max_step_norm), cp))
+
+    def get_y(self):
+        Y = np.zeros((self.N, self.no_dims))
+        _check(lib().fitsne_session_get_y(self._h, _p(Y, _f64p)))
+        return Y
+
+    def set_timing(self, on=True):
+        _check(lib().fitsne_session_set_timing(self._h, int(bool(on))))
+
+    def stage_times(self):
+        out = np.zeros(8)
+        _check(lib().fitsne_session_stage_times(self._h, _p(out, _f64p)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fitsne_session_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,148 @@
+/*
+ * fitsne_gb300 -- C ABI of the GB300 (sm_103a) implementation of FIt-SNE's per-iteration
+ * gradient and input-similarity stage.
+ *
+ * Every entry point is a drop-in for one interface of the reference (KlugerLab/FIt-SNE
+ * v1.2.1, paths relative to that project); the citation is given beside each.
+ *
+ * Conventions
+ *  - Host buffers are owned by the caller unless stated; arrays are row-major.
+ *  - CSR matrices use 32-bit unsigned row pointers and column indices, as the reference.
+ *  - Functions return 0 on success and a negative FITSNE_E* code on failure (the
+ *    reference calls exit() in several of these places; this library never exits).
+ *    fitsne_last_error() gives a message for the calling thread.
+ *  - One GPU (the current CUDA device).  Calls are not re-entrant on one session.
+ *  - The arithmetic precision of the one-shot entry points is selected with
+ *    fitsne_set_precision(): 32 = the FP32 form (double-float coordinates, FP32 spread /
+ *    FFT / gather / attraction, FP64 reductions; the default) or 64 = the plain FP64
+ *    form of the same kernels.  The environment variable FITSNE_PRECISION sets the
+ *    initial value.
+ */
+#ifndef FITSNE_GB300_H
+#define FITSNE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FITSNE_OK 0
+#define FITSNE_E_ARG (-3)         /* invalid argument (the reference exit(1)s on most) */
+#define FITSNE_E_IO (-2)          /* file could not be opened / read (reference returns -2) */
+#define FITSNE_E_UNSUPPORTED (-4) /* option outside this build's scope (exact t-SNE, Barnes-Hut) */
+#define FITSNE_E_CUDA (-10)       /* CUDA runtime error */
+#define FITSNE_E_GRID (-13)       /* interpolation grid larger than the on-chip FFT supports */
+#define FITSNE_E_NOMEM (-20)      /* host allocation failed */
+
+/* ---------------------------------------------------------------------------------
+ * Whole pipeline.  Replaces TSNE::run (src/tsne.h:42-48, src/tsne.cpp:118-592) with the
+ * same arguments and meaning.  X (N x D) is read, not modified (the reference centres and
+ * rescales it in place); Y (N x no_dims) is the initial solution when skip_random_init is
+ * non-zero and receives the embedding; costs (max_iter) receives the KL divergence at
+ * every 50th and the last iteration.  Supported: nbody_algorithm 2 (FFT) with theta != 0;
+ * knn_algo 2 (exact kNN); knn_algo 1 (Annoy) is served by the same exact kNN;
+ * load_affinities 0/1/2 with the reference's P_row.dat / P_col.dat / P_val.dat files in
+ * the working directory.  nthreads is accepted and ignored (the work runs on the GPU).
+ */
+int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexity, double theta, int rand_seed,
+               int skip_random_init, int max_iter, int stop_lying_iter, int mom_switch_iter, double momentum,
+               double final_momentum, double learning_rate, int K, double sigma, int nbody_algorithm,
+               int knn_algo, double early_exag_coeff, double *costs, int no_momentum_during_exag,
+               int start_late_exag_iter, double late_exag_coeff, int n_trees, int search_k, int nterms,
+               double intervals_per_integer, int min_num_intervals, unsigned int nthreads, int load_affinities,
+               int perplexity_list_length, double *perplexity_list, double df, double max_step_norm);
+
+/* ---------------------------------------------------------------------------------
+ * One gradient evaluation.  Replaces the private TSNE methods computeFftGradient,
+ * computeFftGradientVariableDf, computeFftGradientOneD and computeFftGradientOneDVariableDf
+ * (src/tsne.h:67-80, dispatched as in src/tsne.cpp:444-464: no_dims 1 or 2, df == 1 or
+ * not).  P is the CSR (row_P[N+1], col_P[nnz], val_P[nnz]); Y is N x no_dims; dC receives
+ * the gradient (no factor 4, as the reference); *sum_Q receives Z (current_sum_Q).
+ */
+int fitsne_fft_gradient(const unsigned int *row_P, const unsigned int *col_P, const double *val_P,
+                        const double *Y, int N, int no_dims, double *dC, int nterms, double intervals_per_integer,
+                        int min_num_intervals, double df, double *sum_Q);
+
+/* KL divergence over the CSR edges with a given Z.  Replaces TSNE::evaluateErrorFft
+ * (src/tsne.h:92, src/tsne.cpp:1329-1355); the result is the plain sum, without the
+ * exaggeration correction that TSNE::run applies afterwards. */
+int fitsne_evaluate_error_fft(const unsigned int *row_P, const unsigned int *col_P, const double *val_P,
+                              const double *Y, int N, int no_dims, double df, double sum_Q, double *C);
+
+/* ---------------------------------------------------------------------------------
+ * Input similarities. */
+
+/* Exact K nearest neighbours of every row of X (N x D), self included.  Replaces
+ * VpTree::search over all points (src/vptree.h:110-133 with euclidean_distance,
+ * src/vptree.h:97-107): indices[N*K] in increasing distance, distances[N*K] are
+ * non-squared Euclidean distances in FP64. */
+int fitsne_knn(const double *X, int N, int D, int K, unsigned int *indices, double *distances);
+
+/* Row-wise perplexity calibration.  Batched replacement of
+ * TSNE::distances2similarities (src/tsne.h:95-98, src/tsne.cpp:1394-1500) for rows of K
+ * neighbour distances with the point itself already removed, used the way the kNN paths
+ * use it (n = -1, ifSquared = true on non-squared distances, src/tsne.cpp:1692-1693):
+ * P[nrows*K] receives the row-normalised similarities, betas[nrows] (may be NULL) the
+ * precision of the last (or only) perplexity.  perplexity > 0: bisection to that
+ * perplexity; perplexity < 0: fixed sigma; perplexity == 0: average over the list. */
+int fitsne_distances2similarities(const double *D, double *P, int nrows, int K, double perplexity, double sigma,
+                                  int perplexity_list_length, const double *perplexity_list, double *betas);
+
+/* kNN + calibration into fixed-length CSR rows.  Replaces the VP-tree overload of
+ * TSNE::computeGaussianPerplexity (src/tsne.h:105-107, src/tsne.cpp:1643-1726).  The three
+ * arrays are malloc'd here (release with free() or fitsne_free()); row_P[n] = n*K. */
+int fitsne_gaussian_perplexity(const double *X, int N, int D, unsigned int **row_P, unsigned int **col_P,
+                               double **val_P, double perplexity, int K, double sigma, unsigned int nthreads,
+                               int perplexity_list_length, const double *perplexity_list);
+
+/* (P + P^T) / 2 on the union pattern, in the reference's entry order.  Replaces
+ * TSNE::symmetrizeMatrix (src/tsne.h:56, src/tsne.cpp:1730-1828): the input arrays are
+ * freed with free() and replaced by malloc'd output arrays. */
+int fitsne_symmetrize(unsigned int **row_P, unsigned int **col_P, double **val_P, int N);
+
+/* ---------------------------------------------------------------------------------
+ * File formats of the fast_tsne binary (src/tsne.cpp:1895-2038). */
+int fitsne_load_data(const char *data_path, double **data, double **Y, int *n, int *d, int *no_dims,
+                     double *theta, double *perplexity, int *rand_seed, int *max_iter, int *stop_lying_iter,
+                     int *mom_switch_iter, double *momentum, double *final_momentum, double *learning_rate,
+                     int *K, double *sigma, int *nbody_algo, int *knn_algo, double *early_exag_coeff,
+                     int *no_momentum_during_exag, int *n_trees, int *search_k, int *start_late_exag_iter,
+                     double *late_exag_coeff, int *nterms, double *intervals_per_integer, int *min_num_intervals,
+                     int *skip_random_init, int *load_affinities, int *perplexity_list_length,
+                     double **perplexity_list, double *df, double *max_step_norm);
+int fitsne_save_data(const char *result_path, const double *data, const double *costs, int n, int d, int max_iter);
+
+/* ---------------------------------------------------------------------------------
+ * Device-resident optimisation (the iteration loop of TSNE::run, src/tsne.cpp:437-577,
+ * split out so that P and Y stay on the GPU between calls). */
+typedef struct fitsne_session fitsne_session;
+
+/* precision: 32 or 64 (see above). */
+int fitsne_session_create(fitsne_session **out, int N, int no_dims, const unsigned int *row_P,
+                          const unsigned int *col_P, const double *val_P, const double *Y0, int nterms,
+                          double intervals_per_integer, int min_num_intervals, double df, int precision);
+/* Runs iterations [it0, it1) of the schedule; early_exag_coeff must be resolved (> 0).
+ * costs (length >= max_iter, may be NULL) receives the KL at the reference's iterations. */
+int fitsne_session_run(fitsne_session *s, int it0, int it1, int max_iter, int stop_lying_iter,
+                       int mom_switch_iter, double momentum, double final_momentum, double learning_rate,
+                       double early_exag_coeff, int no_momentum_during_exag, int start_late_exag_iter,
+                       double late_exag_coeff, double max_step_norm, double *costs);
+int fitsne_session_get_y(fitsne_session *s, double *Y);
+/* Per-stage device milliseconds of the last iteration when timing is on:
+ * out[0..5] = centre/min-max, spread, FFT convolution, gather, attraction+update, total;
+ * out[6] = boxes per dimension, out[7] = FFT length. */
+int fitsne_session_set_timing(fitsne_session *s, int on);
+int fitsne_session_stage_times(fitsne_session *s, double *out8);
+void fitsne_session_destroy(fitsne_session *s);
+
+/* ---------------------------------------------------------------------------------
+ * Misc. */
+void fitsne_set_precision(int bits);
+int fitsne_get_precision(void);
+const char *fitsne_last_error(void);
+const char *fitsne_version(void); /* "1.2.1" data-file protocol version */
+void fitsne_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
