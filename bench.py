@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""FIt-SNE on one GB300: t-SNE iterations/s at N = 1,000,000, 2-D, and end-to-end seconds.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (both arms): N = 1,000,000 x D = 50 Gaussian mixture (10 clusters, Dirichlet(2)
+weights, per-cluster std U(0.5, 2), centres N(0, 25 I), seed 42); perplexity 30, K = 90,
+2-D, df = 1, learning rate N/12, nterms 3, min_num_intervals 50, intervals_per_integer 1.
+A *step* is one optimiser iteration after the early exaggeration (exaggeration 1,
+momentum 0.8): spread + FFT convolution + gather on the interpolation grid, attraction over
+the ~1.3e8 non-zeros of P, gains/momentum/clipping update, zero-mean.  Steps start from the
+same synthetic expanded embedding (10 clusters, centres N(0, 40^2 I), spread 6), which puts
+the grid at its late-run size (200 boxes per side).
+
+gb300 arm: P is built on the GPU from the data (exact kNN, calibration, symmetrisation) and
+stays resident; W untimed steps, then K steps timed with CUDA events on the library's stream.
+`e2e` runs the whole pipeline (fitsne_run: data on the host -> embedding on the host, 1000
+iterations of the reference schedule) and reports iterations/s over that wall time.
+The FP64 form of the same kernels is timed on the same steps (`plain_fp64`) and the FP32
+gradient is compared with the FP64 one at the starting state (`grad_rel_l2_vs_fp64`).
+
+reference arm: the reference's CPU path (the C restatement in oracle/, the reference tree is
+not on the GPU machine) on all host cores, on the same step definition; P for that arm is built
+on the CPU from random within-cluster neighbour lists of the same size (K = 90 per row,
+symmetrised by the restated symmetrizeMatrix): the exact kNN of 1M points on the CPU takes
+hours.  The number of timed CPU steps is capped so that the arm ends within a few minutes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fit-sne_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "t-SNE iters/s at N=1M 2D vs plain GPU form at grad rel-L2≤1e-4; end-to-end s"
+PERPLEXITY = 30.0
+K_NEIGH = 90
+D_IN = 50
+SCHEDULE = dict(max_iter=1000, stop_lying_iter=250, mom_switch_iter=250, momentum=0.5, final_momentum=0.8,
+                early_exag_coeff=12.0, max_step_norm=5.0)
+STEP_IT0 = 300  # steps are iterations of the post-exaggeration phase
+HBM_FALLBACK_GBS = 6800.0
+
+
+def mixture(N, D=D_IN, seed=42):
+    """10-cluster Gaussian mixture: Dirichlet(2) weights, std U(0.5, 2), centres N(0, 25 I)."""
+    rng = np.random.default_rng(seed)
+    w = rng.dirichlet(np.full(10, 2.0))
+    sizes = rng.multinomial(N, w)
+    labels = np.repeat(np.arange(10), sizes)
+    centres = rng.standard_normal((10, D)) * 5.0
+    std = rng.uniform(0.5, 2.0, 10)
+    X = centres[labels] + rng.standard_normal((N, D)) * std[labels, None]
+    return X, labels, sizes
+
+
+def expanded_state(labels, seed=7):
+    """Synthetic post-exaggeration embedding of the same clusters (extent ~ +-100)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.standard_normal((10, 2)) * 40.0
+    Y = centres[labels] + rng.standard_normal((len(labels), 2)) * 6.0
+    return Y - Y.mean(0)
+
+
+def cpu_sample_P(orc, labels, sizes, K=K_NEIGH, seed=3):
+    """Random within-cluster neighbour lists of K per row, calibrated-like weights,
+    symmetrised by the restated symmetrizeMatrix and normalised."""
+    rng = np.random.default_rng(seed)
+    N = len(labels)
+    starts = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    col = (starts[labels][:, None] + (rng.random((N, K)) * sizes[labels][:, None]).astype(np.int64))
+    col = np.where(col == np.arange(N)[:, None], (col + 1) % N, col).astype(np.uint32).ravel()
+    row = (np.arange(N + 1, dtype=np.int64) * K).astype(np.uint32)
+    val = rng.random(N * K)
+    val /= val.reshape(N, K).sum(1).repeat(K)
+    r, c, v = orc.symmetrize(row, col, val, N)
+    return r, c, v / v.sum()
+
+
+def time_cpu_steps(orc, P, Y, steps, nthreads, budget_s=None):
+    """Runs reference iterations (post-exaggeration parameters); returns (timed, seconds)."""
+    row, col, val = P
+    N = Y.shape[0]
+    Y = Y.copy()
+    uY = np.zeros_like(Y)
+    gains = np.ones_like(Y)
+    lr = N / 12.0
+    done, t0 = 0, time.perf_counter()
+    for _ in range(steps):
+        orc.gradient_step(row, col, val, Y, uY, gains, 3, 1.0, 50, nthreads, 1.0, 1.0, 0.8, lr, 1, 5.0)
+        done += 1
+        if budget_s is not None and time.perf_counter() - t0 > budget_s:
+            break
+    return done, time.perf_counter() - t0
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def attraction_bytes(N, nnz):
+    """Algorithmic bytes of one attraction + update launch (FP32 form, 2-D): row pointers,
+    col (u32) + val (f32) per non-zero, own Y read and new Y write (double-float, 16 B),
+    uY and gains read + write (8 B each), repulsion numerators read (8 B).  Neighbour Y
+    gathers count 0 (Y, 16 MB, stays in L2)."""
+    return 4 * (N + 1) + 8 * nnz + N * (16 + 16 + 16 + 16 + 8)
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build_restated()
+    orc = oracle.Restated()
+    X, labels, sizes = mixture(args.n)
+    del X
+    P = cpu_sample_P(orc, labels, sizes)
+    Y = expanded_state(labels)
+    cores = os.cpu_count() or 1
+    w_done, w_s = time_cpu_steps(orc, P, Y, args.warmup, cores)
+    per = w_s / max(1, w_done)
+    cap = max(1, int(150.0 / max(per, 1e-3)))
+    timed, secs = time_cpu_steps(orc, P, Y, min(args.steps, cap), cores, budget_s=170.0)
+    value = timed / secs
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "steps_timed": timed, "warmup": args.warmup, "ms_per_step": 1e3 * secs / timed,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian mixture; random within-cluster P of the same size)",
+            "config": config(args, "CPU restatement of the reference path"),
+            "cpu_baseline": {"value": value, "unit": "iters/s", "cores": cores, "kind": "port",
+                             "sample": "%d post-exaggeration iterations at N=%d, 2-D" % (timed, args.n)},
+            "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def config(args, impl_note):
+    return {"workload": "N=%d x D=50 Gaussian mixture (10 clusters, seed 42); perplexity 30, K=90, 2-D, df=1, "
+                        "lr=N/12; step = one post-exaggeration FFT-gradient iteration" % args.n,
+            "N": args.n, "D": D_IN, "no_dims": 2, "perplexity": PERPLEXITY, "K": K_NEIGH, "df": 1.0,
+            "nterms": 3, "min_num_intervals": 50, "intervals_per_integer": 1.0,
+            "l2": "inputs larger than L2 (P: ~1 GB per step vs 129 MB L2)", "parallelism": "replicas",
+            "impl": impl_note}
+
+
+def run_gb300(args, world, rank, local):
+    import fitsne
+    hbm, peak_kind = peaks()
+    X, labels, sizes = mixture(args.n)
+    Yst = expanded_state(labels)
+    N = args.n
+    t0 = time.perf_counter()
+    s32 = fitsne.Session.from_data(X, Yst, perplexity=PERPLEXITY, precision=32)
+    setup_s = time.perf_counter() - t0
+    nnz = s32.nnz
+    g32, z32 = s32.gradient()
+    sched = dict(SCHEDULE, learning_rate=N / 12.0)
+    # FP64 form of the same kernels on the same steps
+    s64 = fitsne.Session.from_data(X, Yst, perplexity=PERPLEXITY, precision=64)
+    g64, z64 = s64.gradient()
+    grad_rel = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
+    s64.run(STEP_IT0, STEP_IT0 + args.warmup, **sched)
+    k64 = max(10, min(args.steps, 100))
+    s64.run(STEP_IT0 + args.warmup, STEP_IT0 + args.warmup + k64, **sched)
+    fp64_ms = s64.stage_times()[8]
+    s64.close()
+    fp64_value = k64 / (fp64_ms / 1e3)
+
+    s32.set_timing(True)
+    s32.run(STEP_IT0, STEP_IT0 + args.warmup, **sched)
+    barrier(world)
+    with ClockSampler(local) as clk:
+        t1 = time.perf_counter()
+        s32.run(STEP_IT0 + args.warmup, STEP_IT0 + args.warmup + args.steps, **sched)
+        wall = time.perf_counter() - t1
+    st = s32.stage_times()
+    s32.close()
+    run_ms = reduce_max(st[8], world)
+    value = world * args.steps / (run_ms / 1e3)
+    attr_ms = st[4]
+    abytes = attraction_bytes(N, nnz)
+    achieved = abytes / (attr_ms / 1e3) / 1e9
+
+    # end to end: data on the host -> embedding on the host, full schedule
+    e2e = None
+    if not args.skip_e2e:
+        rng = np.random.default_rng(1)
+        Y0 = rng.standard_normal((N, 2)) * 1e-4
+        os.environ.setdefault("FITSNE_QUIET", "1")
+        t2 = time.perf_counter()
+        Yout, costs = fitsne.run(X, Y0=Y0, perplexity=PERPLEXITY, learning_rate=N / 12.0, knn_algo=2, **SCHEDULE)
+        e2e_s = reduce_max(time.perf_counter() - t2, world)
+        iters = SCHEDULE["max_iter"]
+        e2e = {"value": world * iters / e2e_s, "unit": "iters/s", "seconds": e2e_s,
+               "h2d_bytes_per_step": int((X.nbytes + Y0.nbytes) / iters),
+               "d2h_bytes_per_step": int((Yout.nbytes + 16 * iters + 8 * (iters // 50)) / iters),
+               "note": "whole fitsne_run (similarities + %d iterations), bytes averaged per iteration" % iters,
+               "final_kl": float(costs[-1])}
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        import oracle
+        oracle.build_restated()
+        orc = oracle.Restated()
+        P = cpu_sample_P(orc, labels, sizes)
+        cores = os.cpu_count() or 1
+        time_cpu_steps(orc, P, Yst, 1, cores)
+        n, secs = time_cpu_steps(orc, P, Yst, args.cpu_steps, cores)
+        cpu = {"value": n / secs, "unit": "iters/s", "cores": cores, "kind": "port",
+               "sample": "%d post-exaggeration iterations of the restated reference at N=%d, 2-D" % (n, N)}
+
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": run_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (double-float coordinates, FP64 reductions)",
+            "data": "synthetic (seeded Gaussian mixture)", "config": config(args, "GB300 sm_103a kernels"),
+            "roofline": {"bound": "hbm", "kernel": "attraction + update (k_attr)", "achieved": achieved,
+                         "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "bytes_per_launch": abytes, "ms_per_launch": attr_ms},
+            "stage_ms": {"centre_minmax": st[0], "spread": st[1], "fft_conv": st[2], "gather": st[3],
+                         "attraction_update": st[4], "iteration": st[5], "boxes_per_dim": st[6], "fft_len": st[7]},
+            "nnz": nnz, "wall_ms_per_step": 1e3 * wall / args.steps, "setup_s": setup_s,
+            "plain_fp64": {"value": fp64_value, "unit": "iters/s", "steps": k64, "speedup": value / fp64_value},
+            "grad_rel_l2_vs_fp64": grad_rel, "Z": z32,
+            "gpu_launches": int(st[9]), "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup()
+    if world > 1:
+        if args.impl == "reference":
+            return run_reference(args, world, rank)
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    rc = run_reference(args, world, rank) if args.impl == "reference" else run_gb300(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

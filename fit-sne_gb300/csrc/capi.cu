@@ -8,6 +8,7 @@
 #include "../../include/fitsne_gb300.h"
 #include "capi_internal.h"
 #include "embedding.cuh"
+#include "session.cuh"
 
 namespace fitsne {
 
@@ -92,45 +93,9 @@ int check_grad_args(const unsigned int *row_P, const unsigned int *col_P, const 
 
 }  // namespace
 
-struct SessionBase {
-    virtual ~SessionBase() {}
-    virtual int run(int it0, int it1, const Schedule &s, double *costs) = 0;
-    virtual int get_y(double *Y) = 0;
-    virtual void set_timing(bool on) = 0;
-    virtual void times(double *out8) = 0;
-    virtual std::string error() = 0;
-    cudaStream_t st = nullptr;
-};
-
-template <typename T>
-struct SessionT : SessionBase {
-    Embedding<T> emb;
-    int run(int it0, int it1, const Schedule &s, double *costs) override {
-        return emb.run_schedule(s, it0, it1, costs, false);
-    }
-    int get_y(double *Y) override { return emb.get_Y(Y); }
-    void set_timing(bool on) override { emb.set_timing(on); }
-    void times(double *o) override {
-        const StageTimes &t = emb.last_times();
-        o[0] = t.center;
-        o[1] = t.spread;
-        o[2] = t.conv;
-        o[3] = t.gather;
-        o[4] = t.attract;
-        o[5] = t.total;
-        o[6] = emb.last_geom().nb;
-        o[7] = emb.last_L();
-    }
-    std::string error() override { return emb.error(); }
-};
-
 }  // namespace fitsne
 
 using namespace fitsne;
-
-struct fitsne_session {
-    std::unique_ptr<SessionBase> impl;
-};
 
 extern "C" {
 
@@ -219,6 +184,13 @@ int fitsne_session_run(fitsne_session *s, int it0, int it1, int max_iter, int st
     return 0;
 }
 
+int fitsne_session_gradient(fitsne_session *s, double *dC, double *sum_Q) {
+    if (!s || !s->impl || !dC) return set_error(FITSNE_E_ARG, "null argument");
+    int rc = s->impl->gradient(dC, sum_Q);
+    if (rc) return set_error(rc == -13 ? FITSNE_E_GRID : FITSNE_E_CUDA, s->impl->error());
+    return 0;
+}
+
 int fitsne_session_get_y(fitsne_session *s, double *Y) {
     if (!s || !s->impl || !Y) return set_error(FITSNE_E_ARG, "null argument");
     int rc = s->impl->get_y(Y);
@@ -232,9 +204,9 @@ int fitsne_session_set_timing(fitsne_session *s, int on) {
     return 0;
 }
 
-int fitsne_session_stage_times(fitsne_session *s, double *out8) {
-    if (!s || !s->impl || !out8) return set_error(FITSNE_E_ARG, "null argument");
-    s->impl->times(out8);
+int fitsne_session_stage_times(fitsne_session *s, double *out10) {
+    if (!s || !s->impl || !out10) return set_error(FITSNE_E_ARG, "null argument");
+    s->impl->times(out10);
     return 0;
 }
 

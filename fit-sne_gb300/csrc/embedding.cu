@@ -1,9 +1,12 @@
 // Host driver of the per-iteration kernels (see embedding.cuh).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "embedding.cuh"
+#include "reorder.cuh"
+#include "sort.cuh"
 
 namespace fitsne {
 
@@ -48,7 +51,10 @@ GridGeom make_grid_geom(double mn, double mx, int D, const GridParams &gp) {
 }
 
 template <typename T>
-Embedding<T>::Embedding() {}
+Embedding<T>::Embedding() {
+    const char *e = std::getenv("FITSNE_REORDER");
+    if (e && std::atoi(e) == 0) reorder_enabled_ = false;
+}
 
 template <typename T>
 Embedding<T>::~Embedding() {
@@ -67,10 +73,16 @@ Embedding<T>::~Embedding() {
     cudaFree(work_b_);
     cudaFree(kspec_);
     for (auto &kv : tw_) cudaFree(kv.second);
+    for (void *p : {(void *) perm_, (void *) iperm_, (void *) rkeys_, (void *) rids_, (void *) rkeys2_,
+                    (void *) rids2_, (void *) rlen_, (void *) row2_, (void *) col2_, (void *) val2_, rscratch_})
+        cudaFree(p);
     cudaFree(red_mem_);
     cudaFree(red_cnt_);
     if (h_pin_) cudaFreeHost(h_pin_);
-    for (auto &e : ev_)
+    for (auto &b : evs_)
+        for (auto &e : b)
+            if (e) cudaEventDestroy(e);
+    for (auto &e : evr_)
         if (e) cudaEventDestroy(e);
 }
 
@@ -119,7 +131,9 @@ int Embedding<T>::alloc_common(int N, int D, size_t nnz) {
     red_.mean = red_.z + 1;
     red_.kl = red_.mean + 2;
     FITSNE_CK(cudaMallocHost(&h_pin_, sizeof(double) * 8));
-    for (auto &e : ev_) FITSNE_CK(cudaEventCreate(&e));
+    for (auto &b : evs_)
+        for (auto &e : b) FITSNE_CK(cudaEventCreate(&e));
+    for (auto &e : evr_) FITSNE_CK(cudaEventCreate(&e));
     return 0;
 }
 
@@ -251,26 +265,26 @@ int Embedding<T>::repulsion() {
     const int mode = (gp_.df == 1.0) ? KERNEL_DF1 : KERNEL_VARDF;
     FITSNE_CK(cudaMemsetAsync(grid_in_, 0, sizeof(Cell4<T>) * gridn, st_));
     FITSNE_CK(launch_spread<T>(Y_[cur_], N_, D_, geom_, grid_in_, st_));
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[2], st_));
+    if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][2], st_));
     if (D_ == 2)
         FITSNE_CK(conv2d_launch<T>(grid_in_, grid_out_, M, plan_, tw_[L_], work_a_, work_b_, kspec_, geom_.hk,
                                    gp_.df, mode, st_));
     else
         FITSNE_CK(conv1d_launch<T>(grid_in_, grid_out_, M, plan_, tw_[L_], work_a_, geom_.hk, gp_.df, mode, st_));
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[3], st_));
+    if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][3], st_));
     FITSNE_CK(launch_gather<T>(Y_[cur_], N_, D_, geom_, grid_out_, mode, rep_, red_, st_));
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[4], st_));
+    if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][4], st_));
+    launches_ += 1 + (D_ == 2 ? 5 : 2) + 1;  // spread, convolution passes, gather
     return 0;
 }
 
 template <typename T>
 int Embedding<T>::gradient(double *dC_host, double *sum_Q) {
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[0], st_));
-    FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, mean_pending_ ? 1 : 0, red_, st_));
+    FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, mean_pending_ ? 1 : 0, excl_, red_, st_));
     mean_pending_ = false;
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[1], st_));
     int rc = prepare_grid();
     if (rc) return rc;
+    tpend_ = false;
     rc = repulsion();
     if (rc) return rc;
     UpdateParams p{};
@@ -279,37 +293,113 @@ int Embedding<T>::gradient(double *dC_host, double *sum_Q) {
     p.df = gp_.df;
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_, p,
                                     red_, st_));
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[5], st_));
+    launches_ += 2;
     std::vector<T> tmp((size_t) N_ * D_);
     FITSNE_CK(cudaMemcpyAsync(tmp.data(), dC_, sizeof(T) * tmp.size(), cudaMemcpyDeviceToHost, st_));
     FITSNE_CK(cudaMemcpyAsync(h_pin_ + 2, red_.z, sizeof(double), cudaMemcpyDeviceToHost, st_));
     FITSNE_CK(cudaStreamSynchronize(st_));
-    for (size_t k = 0; k < tmp.size(); ++k) dC_host[k] = (double) tmp[k];
+    if (reordered_) {
+        std::vector<uint32_t> perm;
+        rc = perm_to_host(perm);
+        if (rc) return rc;
+        for (size_t k = 0; k < (size_t) N_; ++k)
+            for (int d = 0; d < D_; ++d) dC_host[(size_t) perm[k] * D_ + d] = (double) tmp[k * D_ + d];
+    } else {
+        for (size_t k = 0; k < tmp.size(); ++k) dC_host[k] = (double) tmp[k];
+    }
     if (sum_Q) *sum_Q = h_pin_[2];
     return 0;
 }
 
 template <typename T>
-int Embedding<T>::step(const UpdateParams &p, bool) {
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[0], st_));
-    FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, mean_pending_ ? 1 : 0, red_, st_));
+int Embedding<T>::perm_to_host(std::vector<uint32_t> &out) {
+    out.resize(N_);
+    FITSNE_CK(cudaMemcpyAsync(out.data(), perm_, sizeof(uint32_t) * N_, cudaMemcpyDeviceToHost, st_));
+    FITSNE_CK(cudaStreamSynchronize(st_));
+    return 0;
+}
+
+// Renumbers the points along a Morton curve of the current embedding (reorder.cuh).
+template <typename T>
+int Embedding<T>::reorder() {
+    const int W = y_width<T>(D_);
+    if (!perm_) {
+        FITSNE_CK(cudaMalloc(&perm_, sizeof(uint32_t) * N_));
+        FITSNE_CK(cudaMalloc(&iperm_, sizeof(uint32_t) * N_));
+        FITSNE_CK(cudaMalloc(&rkeys_, sizeof(uint32_t) * N_));
+        FITSNE_CK(cudaMalloc(&rids_, sizeof(uint32_t) * N_));
+        FITSNE_CK(cudaMalloc(&rkeys2_, sizeof(uint32_t) * N_));
+        FITSNE_CK(cudaMalloc(&rids2_, sizeof(uint32_t) * N_));
+        FITSNE_CK(cudaMalloc(&rlen_, sizeof(uint32_t) * (N_ + 1)));
+        FITSNE_CK(cudaMalloc(&row2_, sizeof(uint32_t) * (N_ + 1)));
+        FITSNE_CK(cudaMalloc(&col2_, sizeof(uint32_t) * (nnz_ ? nnz_ : 1)));
+        FITSNE_CK(cudaMalloc(&val2_, sizeof(T) * (nnz_ ? nnz_ : 1)));
+        const size_t scr = std::max(radix_sort_scratch_bytes(N_), scan_scratch_bytes((size_t) N_ + 1));
+        FITSNE_CK(cudaMalloc(&rscratch_, scr));
+        FITSNE_CK(launch_iota(perm_, N_, st_));
+    }
+    // current bounds (also applies any pending mean shift)
+    FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, mean_pending_ ? 1 : 0, excl_, red_, st_));
     mean_pending_ = false;
-    if (timing_) FITSNE_CK(cudaEventRecord(ev_[1], st_));
+    FITSNE_CK(cudaMemcpyAsync(h_pin_, red_.mnmx, sizeof(double) * 2, cudaMemcpyDeviceToHost, st_));
+    FITSNE_CK(cudaStreamSynchronize(st_));
+    const double lo = h_pin_[0], hi = h_pin_[1];
+    if (!std::isfinite(lo) || !std::isfinite(hi)) {
+        err_ = "embedding coordinates are not finite";
+        return -11;
+    }
+    FITSNE_CK(launch_morton_keys<T>(Y_[cur_], N_, D_, W, lo, hi, rkeys_, rids_, st_));
+    FITSNE_CK(radix_sort_pairs(rkeys_, rids_, rkeys2_, rids2_, (size_t) N_, 32, rscratch_, st_));
+    const uint32_t *order = rids_;
+    FITSNE_CK(launch_invert(order, rkeys2_, N_, st_));  // rkeys2_ = inverse of order
+    // point arrays
+    FITSNE_CK(launch_gather_rows<T>(Y_[cur_], Y_[1 - cur_], order, N_, W, st_));
+    cur_ = 1 - cur_;
+    FITSNE_CK(launch_gather_rows<T>(uY_, rep_, order, N_, D_, st_));
+    std::swap(uY_, rep_);
+    FITSNE_CK(launch_gather_rows<T>(gains_, dC_, order, N_, D_, st_));
+    std::swap(gains_, dC_);
+    // P: rows in the new order, columns renamed
+    FITSNE_CK(launch_perm_lengths(row_, order, N_, rlen_, st_));
+    FITSNE_CK(exclusive_scan_u32(rlen_, row2_, (size_t) N_, rscratch_, st_));
+    FITSNE_CK(launch_perm_csr<T>(row_, col_, val_, order, rkeys2_, row2_, N_, col2_, val2_, st_));
+    std::swap(row_, row2_);
+    std::swap(col_, col2_);
+    std::swap(val_, val2_);
+    // caller index of each internal point, and its inverse
+    FITSNE_CK(launch_compose(perm_, order, rids2_, N_, st_));
+    std::swap(perm_, rids2_);
+    FITSNE_CK(launch_invert(perm_, iperm_, N_, st_));
+    unsigned int e0 = 0;
+    FITSNE_CK(cudaMemcpyAsync(&e0, iperm_, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
+    FITSNE_CK(cudaStreamSynchronize(st_));
+    excl_ = (int) e0;
+    reordered_ = true;
+    return 0;
+}
+
+template <typename T>
+int Embedding<T>::step(const UpdateParams &p, bool) {
+    if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][0], st_));
+    FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, mean_pending_ ? 1 : 0, excl_, red_, st_));
+    mean_pending_ = false;
+    if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][1], st_));
     int rc = prepare_grid();
     if (rc) return rc;
+    // the stream is idle here: the previous iteration's events are complete
+    if (timing_ && tpend_) {
+        read_stage_events(tb_ ^ 1);
+        tpend_ = false;
+    }
     rc = repulsion();
     if (rc) return rc;
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], uY_, gains_, nullptr, rep_, N_, D_, p,
                                     red_, st_));
+    launches_ += 2;  // centre + attraction
     if (timing_) {
-        FITSNE_CK(cudaEventRecord(ev_[5], st_));
-        FITSNE_CK(cudaEventSynchronize(ev_[5]));
-        cudaEventElapsedTime(&times_.center, ev_[0], ev_[1]);
-        cudaEventElapsedTime(&times_.spread, ev_[1], ev_[2]);
-        cudaEventElapsedTime(&times_.conv, ev_[2], ev_[3]);
-        cudaEventElapsedTime(&times_.gather, ev_[3], ev_[4]);
-        cudaEventElapsedTime(&times_.attract, ev_[4], ev_[5]);
-        cudaEventElapsedTime(&times_.total, ev_[0], ev_[5]);
+        FITSNE_CK(cudaEventRecord(evs_[tb_][5], st_));
+        tpend_ = true;
+        tb_ ^= 1;
     }
     cur_ = 1 - cur_;
     mean_pending_ = true;
@@ -317,8 +407,22 @@ int Embedding<T>::step(const UpdateParams &p, bool) {
 }
 
 template <typename T>
+void Embedding<T>::read_stage_events(int b) {
+    float t[6];
+    cudaEventElapsedTime(&t[0], evs_[b][0], evs_[b][1]);
+    cudaEventElapsedTime(&t[1], evs_[b][1], evs_[b][2]);
+    cudaEventElapsedTime(&t[2], evs_[b][2], evs_[b][3]);
+    cudaEventElapsedTime(&t[3], evs_[b][3], evs_[b][4]);
+    cudaEventElapsedTime(&t[4], evs_[b][4], evs_[b][5]);
+    cudaEventElapsedTime(&t[5], evs_[b][0], evs_[b][5]);
+    for (int k = 0; k < 6; ++k) tacc_[k] += t[k];
+    ++tacc_n_;
+}
+
+template <typename T>
 int Embedding<T>::kl(double exag, double *out) {
     FITSNE_CK(launch_kl<T>(row_, col_, val_, Y_[cur_], N_, D_, exag, gp_.df, red_, st_));
+    launches_ += 1;
     FITSNE_CK(cudaMemcpyAsync(h_pin_ + 3, red_.kl, sizeof(double), cudaMemcpyDeviceToHost, st_));
     FITSNE_CK(cudaStreamSynchronize(st_));
     *out = h_pin_[3];
@@ -335,13 +439,18 @@ int Embedding<T>::kl_with_z(double exag, double z, double *out) {
 template <typename T>
 int Embedding<T>::get_Y(double *Y_host) {
     if (mean_pending_) {
-        FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, 1, red_, st_));
+        FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, 1, excl_, red_, st_));
         mean_pending_ = false;
     }
     double *tmp = nullptr;
-    FITSNE_CK(cudaMalloc(&tmp, sizeof(double) * (size_t) N_ * D_));
+    FITSNE_CK(cudaMalloc(&tmp, sizeof(double) * (size_t) N_ * D_ * (reordered_ ? 2 : 1)));
     FITSNE_CK(launch_y_to_double<T>(Y_[cur_], tmp, N_, D_, st_));
-    FITSNE_CK(cudaMemcpyAsync(Y_host, tmp, sizeof(double) * (size_t) N_ * D_, cudaMemcpyDeviceToHost, st_));
+    double *out = tmp;
+    if (reordered_) {
+        out = tmp + (size_t) N_ * D_;
+        FITSNE_CK(launch_scatter_rows<double>(tmp, out, perm_, N_, D_, st_));
+    }
+    FITSNE_CK(cudaMemcpyAsync(Y_host, out, sizeof(double) * (size_t) N_ * D_, cudaMemcpyDeviceToHost, st_));
     FITSNE_CK(cudaStreamSynchronize(st_));
     cudaFree(tmp);
     return 0;
@@ -357,6 +466,11 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
         if (it == s.start_late_exag_iter) mult *= s.late_exag_coeff;
         if (it == s.mom_switch_iter) momentum = s.final_momentum;
     }
+    const unsigned long long l0 = launches_;
+    tpend_ = false;
+    tacc_n_ = 0;
+    for (double &a : tacc_) a = 0.0;
+    FITSNE_CK(cudaEventRecord(evr_[0], st_));
     for (int it = it0; it < it1; ++it) {
         UpdateParams p{};
         p.mode = 1;
@@ -371,6 +485,12 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
         } else {
             p.use_gains = 1;
             p.max_step_norm = s.max_step_norm;
+        }
+        // renumber for locality a few times while the embedding takes shape
+        if (reorder_enabled_ && N_ >= kReorderMinN &&
+            (it == 50 || it == 150 || it == 300 || it == 600 || (!reordered_ && it == it0 && it0 > 50))) {
+            int rr = reorder();
+            if (rr) return rr;
         }
         int rc = step(p, it == 0);
         if (rc) return rc;
@@ -388,6 +508,23 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
             costs[it] = C;
             if (verbose) std::printf("Iteration %d, cost %f\n", it + 1, C);
         }
+    }
+    FITSNE_CK(cudaEventRecord(evr_[1], st_));
+    FITSNE_CK(cudaEventSynchronize(evr_[1]));
+    cudaEventElapsedTime(&times_.run_ms, evr_[0], evr_[1]);
+    times_.launches = launches_ - l0;
+    if (timing_ && tpend_) {
+        read_stage_events(tb_ ^ 1);
+        tpend_ = false;
+    }
+    if (tacc_n_ > 0) {
+        // average per iteration over this call
+        times_.center = (float) (tacc_[0] / tacc_n_);
+        times_.spread = (float) (tacc_[1] / tacc_n_);
+        times_.conv = (float) (tacc_[2] / tacc_n_);
+        times_.gather = (float) (tacc_[3] / tacc_n_);
+        times_.attract = (float) (tacc_[4] / tacc_n_);
+        times_.total = (float) (tacc_[5] / tacc_n_);
     }
     return 0;
 }

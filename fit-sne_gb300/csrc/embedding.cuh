@@ -30,6 +30,9 @@ struct Schedule {
     double max_step_norm = 5.0;
 };
 
+// Embeddings smaller than this are not renumbered (they fit in cache either way).
+constexpr int kReorderMinN = 16384;
+
 struct GridParams {
     int nterms = 3;
     double intervals_per_integer = 1.0;
@@ -40,6 +43,8 @@ struct GridParams {
 // Per-stage device time of the last timed iteration (CUDA events), milliseconds.
 struct StageTimes {
     float center = 0, spread = 0, conv = 0, gather = 0, attract = 0, total = 0;
+    float run_ms = 0;               // device time of the last run_schedule call (events)
+    unsigned long long launches = 0;  // kernels launched by the last run_schedule call
 };
 
 template <typename T>
@@ -119,7 +124,27 @@ class Embedding {
     int L_ = 0;
     bool timing_ = false;
     StageTimes times_;
-    cudaEvent_t ev_[6] = {};
+    // per-iteration stage events, double-buffered so that the previous iteration's events
+    // are read after the next iteration's existing synchronisation (no extra host waits)
+    cudaEvent_t evs_[2][6] = {};
+    cudaEvent_t evr_[2] = {};  // start / end of a run_schedule call
+    int tb_ = 0;
+    bool tpend_ = false;
+    double tacc_[6] = {};
+    int tacc_n_ = 0;
+    void read_stage_events(int buf);
+    unsigned long long launches_ = 0;  // running count of this object's kernel launches
+
+    // locality renumbering (reorder.cuh): perm_[k] = caller index of internal point k
+    int reorder();
+    int perm_to_host(std::vector<uint32_t> &out);
+    bool reorder_enabled_ = true;
+    bool reordered_ = false;
+    int excl_ = 0;  // internal index of the caller's point 0 (min/max rule of the reference)
+    uint32_t *perm_ = nullptr, *iperm_ = nullptr, *rkeys_ = nullptr, *rids_ = nullptr, *rkeys2_ = nullptr,
+             *rids2_ = nullptr, *rlen_ = nullptr, *row2_ = nullptr, *col2_ = nullptr;
+    T *val2_ = nullptr;
+    void *rscratch_ = nullptr;
     std::string err_;
 };
 

@@ -273,7 +273,7 @@ FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *co
 // ---------------------------------------------------------------------------------
 // center (subtract the pending mean) + min/max (tsne.cpp:531, 1039-1049, 769-773)
 template <typename T, int D>
-__global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply_mean, RedScratch r) {
+__global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply_mean, int excl, RedScratch r) {
     typedef typename YL<T, D>::P P;
     __shared__ double sh[2 * 32];
     P negm[D];
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply
             mx = fmax(mx, v);
             // 2-D: the first coordinate of the first point never reaches the min
             // (if / else-if pair of tsne.cpp:1045-1048)
-            if (!(D == 2 && i == 0 && d == 0)) mn = fmin(mn, v);
+            if (!(D == 2 && i == excl && d == 0)) mn = fmin(mn, v);
         }
     }
     if (grid_minmax<2>(mn, mx, r.part, r.count + 0, sh)) {
@@ -622,12 +622,12 @@ inline int grid_for(long long n, int per_block, int cap) {
 }  // namespace
 
 template <typename T>
-cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, RedScratch r, cudaStream_t st) {
+cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, int excl, RedScratch r, cudaStream_t st) {
     const int g = grid_for(N, kBlock, kRedGrid);
     if (D == 2)
-        k_center_minmax<T, 2><<<g, kBlock, 0, st>>>(Y, N, apply_mean, r);
+        k_center_minmax<T, 2><<<g, kBlock, 0, st>>>(Y, N, apply_mean, excl, r);
     else
-        k_center_minmax<T, 1><<<g, kBlock, 0, st>>>(Y, N, apply_mean, r);
+        k_center_minmax<T, 1><<<g, kBlock, 0, st>>>(Y, N, apply_mean, excl, r);
     return cudaGetLastError();
 }
 
@@ -719,7 +719,7 @@ cudaError_t launch_cast_from_double(const double *src, T *dst, size_t n, cudaStr
 }
 
 #define FITSNE_INST(T)                                                                                           \
-    template cudaError_t launch_center_minmax<T>(T *, int, int, int, RedScratch, cudaStream_t);                 \
+    template cudaError_t launch_center_minmax<T>(T *, int, int, int, int, RedScratch, cudaStream_t);                \
     template cudaError_t launch_spread<T>(const T *, int, int, const GridGeom &, Cell4<T> *, cudaStream_t);     \
     template cudaError_t launch_gather<T>(const T *, int, int, const GridGeom &, const Cell4<T> *, int, T *,     \
                                           RedScratch, cudaStream_t);                                            \

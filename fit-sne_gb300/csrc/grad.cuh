@@ -62,8 +62,10 @@ struct UpdateParams {
 };
 
 // --- launchers (T = float: double-float Y of width 2*D; T = double: plain Y) ---------
+// excl: index of the point whose first coordinate is left out of the minimum (the
+// caller's point 0 after any internal renumbering).
 template <typename T>
-cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, RedScratch r, cudaStream_t st);
+cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, int excl, RedScratch r, cudaStream_t st);
 template <typename T>
 cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &g, Cell4<T> *grid, cudaStream_t st);
 template <typename T>

@@ -12,6 +12,7 @@
 #include "capi_internal.h"
 #include "embedding.cuh"
 #include "knn.cuh"
+#include "session.cuh"
 
 namespace fitsne {
 namespace {
@@ -83,6 +84,53 @@ int save_p_files(int N, const std::vector<uint32_t> &row, const std::vector<uint
     return 0;
 }
 
+// Similarity stage of TSNE::run (src/tsne.cpp:153-330): centre and scale X, exact kNN,
+// calibration, symmetrisation, normalisation; P stays on the device.
+int build_P(const double *X, int N, int D, double perplexity, int K, double sigma, int list_len, const double *list,
+            DevCSR *P, cudaStream_t st, bool vb, bool annoy_requested) {
+    std::string err;
+    const bool normalize = perplexity > 0 || list_len > 0;
+    double *Xd = nullptr;
+    if (prepare_X(X, N, D, normalize, &Xd, st, err)) return set_error(FITSNE_E_CUDA, err);
+    int K_use;
+    double sigma_use;
+    if (perplexity < 0) {
+        K_use = K;
+        sigma_use = sigma;
+    } else {
+        if (perplexity > 0) {
+            K_use = (int) (3 * perplexity);
+        } else {
+            K_use = (int) (3 * list[0]);
+            for (int pp = 1; pp < list_len; ++pp)
+                if (3 * list[pp] > K_use) K_use = (int) (3 * list[pp]);
+        }
+        sigma_use = -1;
+    }
+    if (K_use < 1 || K_use + 1 > N) {
+        cudaFree(Xd);
+        return set_error(FITSNE_E_ARG, "number of neighbours must be in [1, N - 1]");
+    }
+    if (vb) {
+        if (annoy_requested) std::printf("Annoy kNN requested: this build computes the exact kNN on the GPU\n");
+        std::printf("Computing input similarities (exact kNN, K = %d) on the GPU...\n", K_use);
+    }
+    DevCSR P0;
+    int rc = gaussian_perplexity_device(Xd, N, D, K_use, perplexity, sigma_use, perplexity == 0 ? list_len : 0, list,
+                                        &P0, st, err);
+    cudaFree(Xd);
+    if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
+    rc = symmetrize_device(P0, P, st, err);
+    free_csr(P0);
+    if (rc) return set_error(FITSNE_E_CUDA, err);
+    double sum = 0.0;
+    if (normalize_device(*P, &sum, st, err)) {
+        free_csr(*P);
+        return set_error(FITSNE_E_CUDA, err);
+    }
+    return 0;
+}
+
 template <typename T>
 int optimise(const DevCSR &P, double *Y, int N, int no_dims, const GridParams &gp, const Schedule &s, double *costs,
              cudaStream_t st, bool vb) {
@@ -143,47 +191,9 @@ int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexit
         if (csr_to_device(row.data(), col.data(), val.data(), N, &P, st.s, err))
             return set_error(FITSNE_E_CUDA, err);
     } else {
-        const bool normalize = perplexity > 0 || perplexity_list_length > 0;
-        double *Xd = nullptr;
-        if (prepare_X(X, N, D, normalize, &Xd, st.s, err)) return set_error(FITSNE_E_CUDA, err);
-        int K_use;
-        double sigma_use;
-        if (perplexity < 0) {
-            K_use = K;
-            sigma_use = sigma;
-        } else {
-            if (perplexity > 0) {
-                K_use = (int) (3 * perplexity);
-            } else {
-                K_use = (int) (3 * perplexity_list[0]);
-                for (int pp = 1; pp < perplexity_list_length; ++pp)
-                    if (3 * perplexity_list[pp] > K_use) K_use = (int) (3 * perplexity_list[pp]);
-            }
-            sigma_use = -1;
-        }
-        if (K_use < 1 || K_use + 1 > N) {
-            cudaFree(Xd);
-            return set_error(FITSNE_E_ARG, "number of neighbours must be in [1, N - 1]");
-        }
-        if (vb) {
-            if (knn_algo == 1) std::printf("Annoy kNN requested: this build computes the exact kNN on the GPU\n");
-            std::printf("Computing input similarities (exact kNN, K = %d) on the GPU...\n", K_use);
-        }
-        DevCSR P0;
-        int krs = 0;
-        rc = gaussian_perplexity_device(Xd, N, D, K_use, perplexity, sigma_use,
-                                        perplexity == 0 ? perplexity_list_length : 0, perplexity_list, &P0, st.s,
-                                        err, &krs);
-        cudaFree(Xd);
-        if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
-        rc = symmetrize_device(P0, &P, st.s, err);
-        free_csr(P0);
-        if (rc) return set_error(FITSNE_E_CUDA, err);
-        double sum = 0.0;
-        if (normalize_device(P, &sum, st.s, err)) {
-            free_csr(P);
-            return set_error(FITSNE_E_CUDA, err);
-        }
+        rc = build_P(X, N, D, perplexity, K, sigma, perplexity_list_length, perplexity_list, &P, st.s, vb,
+                     knn_algo == 1);
+        if (rc) return rc;
     }
     if (load_affinities == 2) {
         if (vb) std::printf("Saving approximate input similarities to files...\n");
@@ -242,6 +252,62 @@ int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexit
         rc = optimise<float>(P, Y, N, no_dims, gp, s, costs, st.s, vb);
     free_csr(P);
     return rc;
+}
+
+int fitsne_session_create_from_data(fitsne_session **out, const double *X, int N, int D, int no_dims,
+                                    double perplexity, int K, double sigma, int perplexity_list_length,
+                                    const double *perplexity_list, const double *Y0, int nterms,
+                                    double intervals_per_integer, int min_num_intervals, double df, int precision,
+                                    unsigned long long *nnz) {
+    if (!out) return set_error(FITSNE_E_ARG, "out is null");
+    *out = nullptr;
+    if (!X || !Y0 || N < 2 || D < 1) return set_error(FITSNE_E_ARG, "invalid data arguments");
+    if (N - 1 < 3 * perplexity) return set_error(FITSNE_E_ARG, "Perplexity too large for the number of data points!");
+    if (no_dims != 1 && no_dims != 2)
+        return set_error(FITSNE_E_ARG, "FFT interpolation scheme supports only 1 or 2 output dimensions");
+    if (nterms < 1 || nterms > kMaxInterp) return set_error(FITSNE_E_ARG, "n_interpolation_points must be in [1, 8]");
+    if (!(intervals_per_integer > 0) || min_num_intervals < 1 || !(df > 0))
+        return set_error(FITSNE_E_ARG, "invalid interpolation grid parameters");
+    if (precision != 32 && precision != 64) return set_error(FITSNE_E_ARG, "precision must be 32 or 64");
+    if (perplexity == 0 && (perplexity_list_length < 1 || !perplexity_list))
+        return set_error(FITSNE_E_ARG, "perplexity 0 needs a perplexity list");
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+        return set_error(FITSNE_E_CUDA, "cudaStreamCreate failed");
+    DevCSR P;
+    rc = build_P(X, N, D, perplexity, K, sigma, perplexity_list_length, perplexity_list, &P, st, false, false);
+    if (rc) {
+        cudaStreamDestroy(st);
+        return rc;
+    }
+    if (nnz) *nnz = P.nnz;
+    GridParams gp;
+    gp.nterms = nterms;
+    gp.intervals_per_integer = intervals_per_integer;
+    gp.min_num_intervals = min_num_intervals;
+    gp.df = df;
+    std::unique_ptr<fitsne_session> s(new fitsne_session);
+    if (precision == 64) {
+        auto *p = new SessionT<double>;
+        s->impl.reset(p);
+        rc = p->emb.init_device(N, no_dims, P.row, P.col, P.val, P.nnz, Y0, gp, st);
+    } else {
+        auto *p = new SessionT<float>;
+        s->impl.reset(p);
+        rc = p->emb.init_device(N, no_dims, P.row, P.col, P.val, P.nnz, Y0, gp, st);
+    }
+    free_csr(P);
+    s->impl->st = st;
+    if (rc) {
+        std::string m = s->impl->error();
+        s->impl.reset();
+        cudaStreamDestroy(st);
+        return set_error(FITSNE_E_CUDA, m);
+    }
+    *out = s.release();
+    return 0;
 }
 
 int fitsne_knn(const double *X, int N, int D, int K, unsigned int *indices, double *distances) {

@@ -53,6 +53,12 @@ _SIGS = {
                                           ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_double, _f64p]),
+    "fitsne_session_create_from_data": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), _f64p, ctypes.c_int,
+                                                       ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                       ctypes.c_double, ctypes.c_int, _f64p, _f64p, ctypes.c_int,
+                                                       ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                       ctypes.POINTER(ctypes.c_ulonglong)]),
+    "fitsne_session_gradient": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p]),
     "fitsne_session_get_y": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
     "fitsne_session_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fitsne_session_stage_times": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
@@ -262,6 +268,39 @@ class Session:
                                            int(precision)))
         self._h = h
 
+    @classmethod
+    def from_data(cls, X, Y0, perplexity=30.0, K=-1, sigma=-1.0, perplexity_list=None, nterms=3,
+                  intervals_per_integer=1.0, min_num_intervals=50, df=1.0, precision=32):
+        """Builds P on the GPU from the data (as TSNE::run does) and keeps it there."""
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        Y0 = np.ascontiguousarray(Y0, dtype=np.float64)
+        if Y0.ndim == 1:
+            Y0 = Y0[:, None]
+        N, D = X.shape
+        pl = np.ascontiguousarray(perplexity_list if perplexity_list is not None else [0.0], dtype=np.float64)
+        npl = 0 if perplexity_list is None else len(perplexity_list)
+        if perplexity_list is not None:
+            perplexity = 0.0
+        self = cls.__new__(cls)
+        self.N, self.no_dims = Y0.shape
+        h = ctypes.c_void_p()
+        nnz = ctypes.c_ulonglong(0)
+        _check(lib().fitsne_session_create_from_data(ctypes.byref(h), _p(X, _f64p), N, D, self.no_dims,
+                                                     float(perplexity), int(K), float(sigma), npl, _p(pl, _f64p),
+                                                     _p(Y0, _f64p), int(nterms), float(intervals_per_integer),
+                                                     int(min_num_intervals), float(df), int(precision),
+                                                     ctypes.byref(nnz)))
+        self._h = h
+        self.nnz = int(nnz.value)
+        return self
+
+    def gradient(self):
+        """Gradient at the current Y without an update: ``(dC, sum_Q)``."""
+        dC = np.zeros((self.N, self.no_dims))
+        z = ctypes.c_double(0.0)
+        _check(lib().fitsne_session_gradient(self._h, _p(dC, _f64p), ctypes.byref(z)))
+        return dC, z.value
+
     def run(self, it0, it1, max_iter=1000, stop_lying_iter=250, mom_switch_iter=250, momentum=0.5,
             final_momentum=0.8, learning_rate=200.0, early_exag_coeff=12.0, no_momentum_during_exag=False,
             start_late_exag_iter=-1, late_exag_coeff=-1.0, max_step_norm=5.0, costs=None):
@@ -281,7 +320,7 @@ class Session:
         _check(lib().fitsne_session_set_timing(self._h, int(bool(on))))
 
     def stage_times(self):
-        out = np.zeros(8)
+        out = np.zeros(10)
         _check(lib().fitsne_session_stage_times(self._h, _p(out, _f64p)))
         return out
 

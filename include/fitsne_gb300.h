@@ -120,6 +120,19 @@ typedef struct fitsne_session fitsne_session;
 int fitsne_session_create(fitsne_session **out, int N, int no_dims, const unsigned int *row_P,
                           const unsigned int *col_P, const double *val_P, const double *Y0, int nterms,
                           double intervals_per_integer, int min_num_intervals, double df, int precision);
+/* As fitsne_session_create, but P is built on the device from the data X (N x D, read
+ * only): centring and max-abs scaling, exact kNN, calibration, symmetrisation and
+ * normalisation exactly as fitsne_run does (the first half of TSNE::run,
+ * src/tsne.cpp:153-330); P never visits the host.  *nnz (may be NULL) receives the number
+ * of non-zeros of P. */
+int fitsne_session_create_from_data(fitsne_session **out, const double *X, int N, int D, int no_dims,
+                                    double perplexity, int K, double sigma, int perplexity_list_length,
+                                    const double *perplexity_list, const double *Y0, int nterms,
+                                    double intervals_per_integer, int min_num_intervals, double df, int precision,
+                                    unsigned long long *nnz);
+/* One gradient evaluation at the session's current Y (no update): dC (N x no_dims) and Z,
+ * as fitsne_fft_gradient. */
+int fitsne_session_gradient(fitsne_session *s, double *dC, double *sum_Q);
 /* Runs iterations [it0, it1) of the schedule; early_exag_coeff must be resolved (> 0).
  * costs (length >= max_iter, may be NULL) receives the KL at the reference's iterations. */
 int fitsne_session_run(fitsne_session *s, int it0, int it1, int max_iter, int stop_lying_iter,
@@ -129,9 +142,11 @@ int fitsne_session_run(fitsne_session *s, int it0, int it1, int max_iter, int st
 int fitsne_session_get_y(fitsne_session *s, double *Y);
 /* Per-stage device milliseconds of the last iteration when timing is on:
  * out[0..5] = centre/min-max, spread, FFT convolution, gather, attraction+update, total;
- * out[6] = boxes per dimension, out[7] = FFT length. */
+ * out[6] = boxes per dimension, out[7] = FFT length; always: out[8] = device milliseconds
+ * of the whole last fitsne_session_run call (CUDA events on the session's stream),
+ * out[9] = number of kernels that call launched. */
 int fitsne_session_set_timing(fitsne_session *s, int on);
-int fitsne_session_stage_times(fitsne_session *s, double *out8);
+int fitsne_session_stage_times(fitsne_session *s, double *out10);
 void fitsne_session_destroy(fitsne_session *s);
 
 /* ---------------------------------------------------------------------------------

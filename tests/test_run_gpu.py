@@ -1,0 +1,102 @@
+"""Whole pipeline (fitsne_run, the TSNE::run replacement) against the reference and the
+C restatement.  Final-KL criterion: within 1% of the reference."""
+import ctypes
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+IDX = [49, 99, 149, 199, 249, 299]
+
+
+@pytest.fixture(scope="module")
+def orc():
+    oracle.build_restated()
+    return oracle.Restated()
+
+
+@pytest.mark.parametrize("bits,early_rtol", [(32, 2e-3), (64, 1e-8)])
+def test_run_final_kl_matches_reference(gpu_lib, golden, bits, early_rtol):
+    """KL within 1% of the reference at every checkpoint.  The optimiser (sign-based gains,
+    momentum) amplifies rounding differences chaotically once the exaggeration ends, so
+    only the first checkpoint is held to a rounding-level tolerance."""
+    gpu_lib.set_precision(bits)
+    try:
+        Y, costs = gpu_lib.run(golden["e2e_X"], Y0=golden["e2e_Y0"], perplexity=15.0, max_iter=300,
+                               stop_lying_iter=100, mom_switch_iter=100, learning_rate=200.0, knn_algo=2)
+    finally:
+        gpu_lib.set_precision(32)
+    ref = golden["e2e_costs"]
+    assert abs(costs[49] - ref[49]) <= early_rtol * ref[49]
+    assert np.all(np.abs(costs[IDX] - ref[IDX]) <= 1e-2 * np.abs(ref[IDX]))
+    assert np.isfinite(Y).all() and np.abs(Y.mean(0)).max() < 1e-6
+
+
+def test_run_random_init_uses_the_reference_generator(gpu_lib):
+    """With no initial Y the solution starts from srand(seed) + the polar method * 1e-4."""
+    X = np.random.default_rng(0).standard_normal((300, 5))
+    Y, _ = gpu_lib.run(X, perplexity=10.0, rand_seed=17, max_iter=0)
+    libc = ctypes.CDLL(None)
+    libc.srand(17)
+    RAND_MAX = 2147483647
+    out = []
+    while len(out) < 600:
+        while True:
+            x = 2 * (libc.rand() / (RAND_MAX + 1.0)) - 1
+            y = 2 * (libc.rand() / (RAND_MAX + 1.0)) - 1
+            r = x * x + y * y
+            if r < 1.0 and r != 0.0:
+                break
+        out.append(x * math.sqrt(-2 * math.log(r) / r) * 1e-4)
+    assert np.allclose(Y.ravel(), out, rtol=1e-14, atol=0)
+
+
+@pytest.mark.parametrize("case", ["late_exag_1d_df05", "no_momentum_2d", "auto_exag", "perp_list_df3"])
+def test_run_options_match_restatement(gpu_lib, orc, case):
+    rng = np.random.default_rng(11)
+    X = np.concatenate([rng.standard_normal((200, 8)) + c for c in (0, 4, 8, 12)])
+    kw = dict(perplexity=12.0, max_iter=600, stop_lying_iter=100, mom_switch_iter=100, learning_rate=200.0)
+    nd = 2
+    if case == "late_exag_1d_df05":
+        kw.update(start_late_exag_iter=150, late_exag_coeff=4.0, df=0.5)
+        nd = 1
+    elif case == "no_momentum_2d":
+        kw.update(no_momentum_during_exag=1, max_step_norm=-1.0)
+    elif case == "auto_exag":
+        kw.update(early_exag_coeff=0.0)
+    else:
+        kw.update(perplexity=0.0, perplexity_list=[5.0, 20.0], df=3.0)
+    Y0 = rng.standard_normal((len(X), nd)) * 1e-4
+    gkw = dict(kw)
+    Y, costs = gpu_lib.run(X, no_dims=nd, Y0=Y0, **gkw)
+    okw = dict(kw)
+    Yo, co = orc.run(X, Y0, no_dims=nd, nthreads=4, **okw)
+    # close while exaggerated; final KL (near convergence) within 1%
+    assert abs(costs[99] - co[99]) <= 3e-3 * co[99]
+    assert abs(costs[599] - co[599]) <= 1e-2 * co[599]
+
+
+def test_affinity_files_save_and_load(gpu_lib, golden, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    X, Y0 = golden["e2e_X"], golden["e2e_Y0"]
+    kw = dict(Y0=Y0, perplexity=15.0, max_iter=100, stop_lying_iter=50, mom_switch_iter=50, learning_rate=200.0)
+    Ya, ca = gpu_lib.run(X, load_affinities=2, **kw)
+    for f in ("P_row.dat", "P_col.dat", "P_val.dat"):
+        assert os.path.getsize(f) > 0
+    row = np.fromfile("P_row.dat", np.uint32)
+    val = np.fromfile("P_val.dat", np.float64)
+    assert len(row) == len(X) + 1 and abs(val.sum() - 1.0) < 1e-12
+    col = np.fromfile("P_col.dat", np.uint32)
+    Yb, cb = gpu_lib.run(X, load_affinities=1, **kw)
+    # the loaded P is the saved one; FP32 runs are not bitwise repeatable (float atomics)
+    gpu_lib.set_precision(64)
+    try:
+        dC1, z1 = gpu_lib.fft_gradient(row, col, val, Y0, 3, 1.0, 50, 1.0)
+    finally:
+        gpu_lib.set_precision(32)
+    assert np.isfinite(dC1).all() and z1 > 0
+    assert abs(ca[49] - cb[49]) <= 1e-2 * ca[49]

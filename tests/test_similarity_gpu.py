@@ -1,0 +1,84 @@
+"""GPU input-similarity stage vs the reference (fixtures) and the C restatement."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def orc():
+    oracle.build_restated()
+    return oracle.Restated()
+
+
+def test_knn_matches_reference_neighbour_lists(gpu_lib, golden):
+    X = golden["sim_X"]
+    K = int(golden["sim_K"])
+    idx, dist = gpu_lib.knn(X, K + 1)
+    assert np.array_equal(idx[:, 0], np.arange(len(X)))
+    # the reference's VP-tree lists, nearest first (this data has no distance ties)
+    assert np.array_equal(idx[:, 1:], golden["knn_col"].reshape(-1, K))
+    assert np.all(np.diff(dist, axis=1) >= 0)
+
+
+@pytest.mark.parametrize("N,D,K", [(3000, 100, 31), (2500, 7, 15), (700, 50, 200)])
+def test_knn_is_exact_against_bruteforce(gpu_lib, orc, N, D, K):
+    rng = np.random.default_rng(N + D)
+    X = rng.standard_normal((N, D)) * rng.uniform(0.1, 2.0, D)
+    X[5] = X[7]  # a duplicate pair: a distance tie at zero
+    idx, dist = gpu_lib.knn(X, K)
+    oidx, odist = orc.knn(X, K, 4)
+    assert np.allclose(dist, odist, rtol=1e-13, atol=1e-15)
+    # index lists agree except within groups of equal distances
+    diff = np.nonzero((idx != oidx).any(axis=1))[0]
+    for r in diff:
+        assert np.allclose(np.sort(dist[r]), np.sort(odist[r]), rtol=1e-13)
+        assert set(idx[r][dist[r] < odist[r][-1]]) == set(oidx[r][odist[r] < odist[r][-1]])
+
+
+def test_calibration_matches_reference(gpu_lib, golden):
+    X = golden["sim_X"]
+    K = int(golden["sim_K"])
+    _, dist = gpu_lib.knn(X, K + 1)
+    P, betas = gpu_lib.distances2similarities(dist[:, 1:], float(golden["sim_perp"]))
+    assert np.allclose(P.ravel(), golden["knn_val"], rtol=1e-12, atol=1e-300)
+    H = -(P * np.log(P)).sum(1)
+    assert np.abs(H - np.log(float(golden["sim_perp"]))).max() < 1e-5 + 1e-12
+
+
+def test_gaussian_perplexity_matches_reference(gpu_lib, golden):
+    X = golden["sim_X"]
+    row, col, val = gpu_lib.gaussian_perplexity(X, float(golden["sim_perp"]), int(golden["sim_K"]))
+    assert np.array_equal(row, golden["knn_row"]) and np.array_equal(col, golden["knn_col"])
+    assert np.allclose(val, golden["knn_val"], rtol=1e-12)
+    _, lcol, lval = gpu_lib.gaussian_perplexity(X, 0.0, 45, perplexity_list=list(golden["list_perps"]))
+    assert np.array_equal(lcol, golden["list_col"]) and np.allclose(lval, golden["list_val"], rtol=1e-12)
+    _, fcol, fval = gpu_lib.gaussian_perplexity(X, -1.0, int(golden["sigma_K"]), sigma=float(golden["sigma"]))
+    assert np.array_equal(fcol, golden["sigma_col"]) and np.allclose(fval, golden["sigma_val"], rtol=1e-12)
+
+
+def test_symmetrize_matches_reference_exactly(gpu_lib, golden):
+    r, c, v = gpu_lib.symmetrize(golden["knn_row"], golden["knn_col"], golden["knn_val"], 2000)
+    assert np.array_equal(r, golden["sym_row"]) and np.array_equal(c, golden["sym_col"])
+    assert np.array_equal(v, golden["sym_val"])
+
+
+@pytest.mark.parametrize("N,kmax,seed", [(500, 9, 0), (20000, 30, 1)])
+def test_symmetrize_general_csr_matches_oracle(gpu_lib, orc, N, kmax, seed):
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, kmax + 1, N)
+    row = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint32)
+    cols = []
+    for i in range(N):
+        c = rng.choice(N, lens[i], replace=False)
+        if i % 97 == 0 and lens[i] > 0 and i not in c:
+            c[0] = i  # self loops appear with duplicate points
+        cols.append(c)
+    col = np.concatenate(cols).astype(np.uint32)
+    val = rng.random(len(col))
+    a = gpu_lib.symmetrize(row, col, val, N)
+    b = orc.symmetrize(row, col, val, N)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
