@@ -1,6 +1,9 @@
 // Input-similarity kernels (see affinity.cuh).
 #include <cfloat>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -305,6 +308,10 @@ __global__ void k_row_sums_max(const uint32_t *__restrict__ row, const double *_
     if ((threadIdx.x & 31) == 0) atomicMax(mx, (unsigned long long) __double_as_longlong(m));
 }
 
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 int key_bits_for(int N) {
     int b = 1;
     while (b < 32 && (1u << b) < (unsigned) N) ++b;
@@ -383,7 +390,11 @@ int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double per
     ACK(cudaMalloc(&dist, sizeof(double) * (size_t) N * (K + 1)));
     KnnStats ks;
     const char *kerr = nullptr;
+    const bool tm = timing_requested();
+    const double t0 = now_s();
     int rc = knn_exact(Xd, N, D, K + 1, idx, dist, st, &ks, &kerr);
+    if (tm) std::fprintf(stderr, "[fitsne] kNN (K=%d): %.3f s, rows rescanned %d\n", K + 1, now_s() - t0,
+                         ks.rows_rescanned);
     if (rc) {
         err = kerr ? kerr : "kNN failed";
         cudaFree(idx);
@@ -399,7 +410,9 @@ int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double per
     ACK(cudaMalloc(&P.val, sizeof(double) * P.nnz));
     k_knn_to_csr<<<4096, 256, 0, st>>>(idx, N, K, P.row, P.col);
     ACK(cudaGetLastError());
+    const double t1 = now_s();
     rc = calibrate_rows(dist, K + 1, 1, P.val, N, K, perplexity, sigma, list_len, list_host, nullptr, st, err);
+    if (tm) std::fprintf(stderr, "[fitsne] calibration: %.3f s\n", now_s() - t1);
     cudaFree(idx);
     cudaFree(dist);
     if (rc) {

@@ -11,11 +11,18 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 
 #include <cuda_runtime.h>
 
 namespace fitsne {
+
+// FITSNE_TIMING=1 in the environment prints the similarity-stage phase times to stderr.
+inline bool timing_requested() {
+    const char *e = std::getenv("FITSNE_TIMING");
+    return e && std::atoi(e) != 0;
+}
 
 // CSR on the device; free with free_csr.
 struct DevCSR {

@@ -1,4 +1,5 @@
 // C ABI: TSNE::run replacement and the input-similarity entry points.
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -120,9 +121,13 @@ int build_P(const double *X, int N, int D, double perplexity, int K, double sigm
                                         &P0, st, err);
     cudaFree(Xd);
     if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
+    const auto t0 = std::chrono::steady_clock::now();
     rc = symmetrize_device(P0, P, st, err);
     free_csr(P0);
     if (rc) return set_error(FITSNE_E_CUDA, err);
+    if (timing_requested())
+        std::fprintf(stderr, "[fitsne] symmetrisation: %.3f s (nnz %zu)\n",
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), P->nnz);
     double sum = 0.0;
     if (normalize_device(*P, &sum, st, err)) {
         free_csr(*P);
