@@ -63,6 +63,10 @@ _SIGS = {
     "fitsne_session_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fitsne_session_stage_times": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
     "fitsne_session_destroy": (None, [ctypes.c_void_p]),
+    "fitsne_fft_gradient_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                   ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                                   _f64p, ctypes.c_void_p]),
     "fitsne_set_precision": (None, [ctypes.c_int]),
     "fitsne_get_precision": (ctypes.c_int, []),
     "fitsne_last_error": (ctypes.c_char_p, []),

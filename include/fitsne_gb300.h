@@ -150,6 +150,31 @@ int fitsne_session_stage_times(fitsne_session *s, double *out10);
 void fitsne_session_destroy(fitsne_session *s);
 
 /* ---------------------------------------------------------------------------------
+ * Gradient evaluation that allocates no device memory.  This entry point has no
+ * counterpart in the reference; it exists for callers that cannot let a library call
+ * cudaMalloc: a host framework that owns the device memory through its own pool or a
+ * fixed budget, or an inner loop where an allocation (and the device synchronisation it
+ * brings) is not allowed.
+ *
+ * Same computation and result as fitsne_fft_gradient in the FP32 form, on the caller's
+ * DEVICE buffers: d_row_P[N+1], d_col_P[nnz], d_val_P[nnz] (float), d_Y[N*no_dims] (double)
+ * in; d_dC[N*no_dims] (double) out; *sum_Q (host, may be NULL) receives Z.  stream is a
+ * cudaStream_t (NULL = the legacy default stream); the call returns after a host
+ * synchronisation on it.  All temporaries come from one fixed device array of 32 MiB that
+ * every GPU loading this library holds until the process exits.  Limits: N <= 262144;
+ * at most 100 boxes per dimension in 2-D (the embedding's extent / intervals_per_integer,
+ * or min_num_intervals, must stay at or below 100) and at most 4096 interpolation nodes in
+ * 1-D; larger inputs are rejected with FITSNE_E_ARG or FITSNE_E_GRID and a message.  The
+ * array is shared by all calls on a device and keeps the last call's contents (each call
+ * clears what must start at zero): calls whose work overlaps on the GPU race on it.  The
+ * first call on a device looks up the array's address with that device current; make it
+ * before any stream capture. */
+int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const unsigned int *d_col_P, const float *d_val_P,
+                                const double *d_Y, int N, int no_dims, double *d_dC, int nterms,
+                                double intervals_per_integer, int min_num_intervals, double df, double *sum_Q,
+                                void *stream);
+
+/* ---------------------------------------------------------------------------------
  * Misc. */
 void fitsne_set_precision(int bits);
 int fitsne_get_precision(void);
