@@ -73,6 +73,7 @@ template <>
 struct BoxP<float> {
     df32 neg_mn, bw;
     float inv_bw, bwT;
+    double mn64, bw64;  // the FP64 geometry, for points on a box edge
     int nb, nterms, M;
     float s[kMaxInterp], inv_den[kMaxInterp];
 };
@@ -89,6 +90,8 @@ BoxP<float> make_box(const GridGeom &g, float *) {
     b.bw = df_from_double(g.bw);
     b.inv_bw = (float) (1.0 / g.bw);
     b.bwT = (float) g.bw;
+    b.mn64 = g.mn;
+    b.bw64 = g.bw;
     b.nb = g.nb;
     b.nterms = g.nterms;
     b.M = g.M;
@@ -114,11 +117,21 @@ BoxP<double> make_box(const GridGeom &g, double *) {
 }
 
 // box index (truncated and clamped as in n_body_fft_2d, nbodyfft.cpp:82-114) and the
-// in-box coordinate t = (x - lower) / width
+// in-box coordinate t = (x - lower) / width.
+// The float quotient q carries a relative error below 3 * 2^-24.  When that error could
+// move q across an integer, the index is taken from the FP64 quotient (x - min) / width
+// that the reference computes, so that both forms interpolate every point from the same
+// box: a point on an edge interpolated from the neighbouring box changes its own and its
+// neighbours' repulsion by the interpolation error (about 1e-2 of a near-field term),
+// far above FP32 rounding.
 FITSNE_D void box_coord(df32 c, const BoxP<float> &b, int &k, float &t) {
     const df32 d = df_add(c, b.neg_mn);
     const float q = (d.hi + d.lo) * b.inv_bw;
     k = (int) q;
+    const float fr = q - (float) k;
+    const float tol = 4e-7f * fabsf(q);
+    if (fr < tol || fr > 1.f - tol)  // (every q < 0 takes this branch too)
+        k = (int) ((((double) c.hi + (double) c.lo) - b.mn64) / b.bw64);
     if (k >= b.nb) k = b.nb - 1;
     else if (k < 0) k = 0;
     df32 p = two_prod((float) k, b.bw.hi);
@@ -419,7 +432,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 // One warp per row; rows are strided over a fixed grid so that the mean of the new Y
 // reduces over few partials.
 template <typename T, int D>
-__global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+__global__ void __launch_bounds__(kBlock, 6) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
                                                  const T *__restrict__ val, const T *__restrict__ Yin,
                                                  T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
                                                  T *__restrict__ dC, const T *__restrict__ rep, int N,
@@ -427,8 +440,12 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
     typedef typename YL<T, D>::P P;
     __shared__ double sh[2 * 32];
     const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
+    // each block walks a contiguous range of rows, its warps on consecutive rows: after the
+    // locality renumbering those rows share most neighbours, so the Y gathers hit in L1
+    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const int rows_pb = (N + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * rows_pb;
+    const int r1 = min(N, r0 + rows_pb);
     const double Zd = *r.z;
     const T zinv = T(1.0 / Zd);
     const T df = T(p.df);
@@ -442,7 +459,7 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
         else
             msum[d] = 0.0;
     }
-    for (int i = gw; i < N; i += nw) {
+    for (int i = r0 + wib; i < r1; i += wpb) {
         P ci[D];
         YL<T, D>::load(Yin, i, ci);
         T a[D];
@@ -552,13 +569,15 @@ __global__ void __launch_bounds__(kBlock) k_kl(const uint32_t *__restrict__ row,
     typedef typename YL<T, D>::P P;
     __shared__ double sh[32];
     const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const int rows_pb = (N + gridDim.x - 1) / gridDim.x;
+    const int r0 = blockIdx.x * rows_pb;
+    const int r1 = min(N, r0 + rows_pb);
     const T zinv = T(1.0 / *r.z);
     const T df = T(dfd);
     const T ex = T(exag);
     double acc[1] = {0.0};
-    for (int i = gw; i < N; i += nw) {
+    for (int i = r0 + wib; i < r1; i += wpb) {
         P ci[D];
         YL<T, D>::load(Y, i, ci);
         const uint32_t e1 = row[i + 1];

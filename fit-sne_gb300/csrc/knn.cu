@@ -1,10 +1,13 @@
 // Exact kNN: FP32 candidate scan + FP64 re-rank with verification (see knn.cuh).
 #include <cfloat>
 #include <cmath>
+#include <cstdlib>
+#include <chrono>
 #include <string>
 #include <vector>
 
 #include "knn.cuh"
+#include "knn_tc.cuh"
 
 namespace fitsne {
 namespace {
@@ -14,6 +17,7 @@ constexpr int kRefTile = 64;
 constexpr int kDChunk = 64;
 constexpr int kStride = kDChunk + 4;  // 17 float4 units per row: conflict-free 16-byte loads
 constexpr int kSlack = 16;
+constexpr int kTcSlack = 29;  // longer lists for the coarser tensor-core distances
 
 __device__ __forceinline__ bool pair_gt(float a, uint32_t ia, float b, uint32_t ib) {
     return a > b || (a == b && ia > ib);
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ X
                                                     const int *__restrict__ qlist, int nq,
                                                     const float *__restrict__ cand_d,
                                                     const uint32_t *__restrict__ cand_i,
-                                                    const double *__restrict__ norms, double maxnorm,
+                                                    const double *__restrict__ norms, double maxnorm, int tc,
                                                     uint32_t *__restrict__ idx, double *__restrict__ dist,
                                                     int *__restrict__ flag) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -234,7 +238,11 @@ __global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ X
             // every point outside the list has an FP32 squared distance >= the C-th one
             const double sC = (double) cand_d[(size_t) slot * C + C - 1];
             const double u = 5.9604644775390625e-08;  // 2^-24
-            const double eps = 1.5 * ((D + 4) * u * sC + 4.0 * u * sqrt(sC) * (norms[q] + maxnorm)) + 1e-30;
+            const double nq = norms[q];
+            // FP32 direct differences (SIMT scan) or BF16 hi/lo tensor-core products (knn_tc.cuh)
+            const double eps =
+                tc ? 1.5 * (D + 4) * u * sC + 8e-5 * nq * maxnorm + 4e-7 * (nq * nq + maxnorm * maxnorm) + 1e-30
+                   : 1.5 * ((D + 4) * u * sC + 4.0 * u * sqrt(sC) * (nq + maxnorm)) + 1e-30;
             const double sK = ed[K - 1] * ed[K - 1];
             ok = (sK < sC - eps) ? 1 : 0;
         }
@@ -295,25 +303,27 @@ cudaError_t dispatch_cand(int cap, const float *Xf, int N, int Dp, int C, const 
 
 template <int CP>
 cudaError_t launch_rerank(const double *Xd, int N, int D, int K, int C, const int *qlist, int nq, const float *cd,
-                          const uint32_t *ci, const double *norms, double maxnorm, uint32_t *idx, double *dist,
-                          int *flag, cudaStream_t st) {
+                          const uint32_t *ci, const double *norms, double maxnorm, int tc, uint32_t *idx,
+                          double *dist, int *flag, cudaStream_t st) {
     const size_t sm = 4 * (size_t) CP * (sizeof(double) + sizeof(uint32_t));
     cudaError_t e = cudaFuncSetAttribute(k_knn_rerank<CP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
     if (e != cudaSuccess) return e;
-    k_knn_rerank<CP><<<(nq + 3) / 4, 128, sm, st>>>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist,
-                                                     flag);
+    k_knn_rerank<CP><<<(nq + 3) / 4, 128, sm, st>>>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, tc, idx,
+                                                     dist, flag);
     return cudaGetLastError();
 }
 
 cudaError_t dispatch_rerank(int cp, const double *Xd, int N, int D, int K, int C, const int *qlist, int nq,
-                            const float *cd, const uint32_t *ci, const double *norms, double maxnorm, uint32_t *idx,
-                            double *dist, int *flag, cudaStream_t st) {
+                            const float *cd, const uint32_t *ci, const double *norms, double maxnorm, int tc,
+                            uint32_t *idx, double *dist, int *flag, cudaStream_t st) {
     switch (cp) {
-        case 128: return launch_rerank<128>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
-        case 256: return launch_rerank<256>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
-        case 512: return launch_rerank<512>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
-        case 1024: return launch_rerank<1024>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
-        case 2048: return launch_rerank<2048>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag, st);
+        case 128: return launch_rerank<128>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, tc, idx, dist, flag, st);
+        case 256: return launch_rerank<256>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, tc, idx, dist, flag, st);
+        case 512: return launch_rerank<512>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, tc, idx, dist, flag, st);
+        case 1024:
+            return launch_rerank<1024>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, tc, idx, dist, flag, st);
+        case 2048:
+            return launch_rerank<2048>(Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, tc, idx, dist, flag, st);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -378,11 +388,42 @@ int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist
     double maxnorm = 0.0;
     for (double v : hn) maxnorm = v > maxnorm ? v : maxnorm;
 
-    // first pass over all rows
-    KCK(cudaMalloc(&cd, sizeof(float) * (size_t) N * C));
-    KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) N * C));
-    KCK(dispatch_cand(cap, Xf, N, Dp, C, nullptr, N, cd, ci, st));
-    KCK(dispatch_rerank(pow2_at_least(C), Xd, N, D, K, C, nullptr, N, cd, ci, norms, maxnorm, idx, dist, flag, st));
+    // first pass over all rows: tensor-core candidates where the device and the shape allow,
+    // else the FP32 scan; both are verified by the FP64 re-rank
+    const auto clk0 = std::chrono::steady_clock::now();
+    auto secs = [&clk0]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - clk0).count(); };
+    const char *mode = std::getenv("FITSNE_KNN");
+    const bool force_simt = mode && std::string(mode) == "simt";
+    const int Ctc = K + kTcSlack < N ? K + kTcSlack : N;
+    const bool use_tc = !force_simt && N >= 256 && knn_tc_supported(D, Ctc);
+    if (use_tc) {
+        C = Ctc;
+        cap = cap_for(C);
+        KCK(cudaMalloc(&cd, sizeof(float) * (size_t) N * C));
+        KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) N * C));
+        std::string terr;
+        if (knn_candidates_tc(Xd, N, D, C, cd, ci, st, terr) != 0) {
+            msg = terr;
+            if (err) *err = msg.c_str();
+            cudaFree(Xf);
+            cudaFree(cd);
+            cudaFree(ci);
+            cudaFree(norms);
+            cudaFree(flag);
+            cudaFree(qlist);
+            return -10;
+        }
+        if (stats) stats->s_candidates = secs();
+        KCK(dispatch_rerank(pow2_at_least(C), Xd, N, D, K, C, nullptr, N, cd, ci, norms, maxnorm, 1, idx, dist, flag,
+                            st));
+    } else {
+        KCK(cudaMalloc(&cd, sizeof(float) * (size_t) N * C));
+        KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) N * C));
+        KCK(dispatch_cand(cap, Xf, N, Dp, C, nullptr, N, cd, ci, st));
+        KCK(dispatch_rerank(pow2_at_least(C), Xd, N, D, K, C, nullptr, N, cd, ci, norms, maxnorm, 0, idx, dist, flag,
+                            st));
+    }
+    if (stats) stats->tensor_cores = use_tc;
     std::vector<int> hf(N);
     KCK(cudaMemcpyAsync(hf.data(), flag, sizeof(int) * N, cudaMemcpyDeviceToHost, st));
     KCK(cudaStreamSynchronize(st));
@@ -390,6 +431,8 @@ int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist
     for (int i = 0; i < N; ++i)
         if (hf[i]) bad.push_back(i);
     if (stats) stats->rows_rescanned = (int) bad.size();
+    const double s_first = secs();
+    if (stats) stats->s_first_pass = s_first;
     // rescans of the unverified rows with longer lists
     while (!bad.empty() && C < N && cap < 2048) {
         C = C * 4 < N ? C * 4 : N;
@@ -404,7 +447,7 @@ int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist
         KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) nq * C));
         KCK(cudaMemcpyAsync(qlist, bad.data(), sizeof(int) * nq, cudaMemcpyHostToDevice, st));
         KCK(dispatch_cand(cap, Xf, N, Dp, C, qlist, nq, cd, ci, st));
-        KCK(dispatch_rerank(pow2_at_least(C), Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, idx, dist, flag,
+        KCK(dispatch_rerank(pow2_at_least(C), Xd, N, D, K, C, qlist, nq, cd, ci, norms, maxnorm, 0, idx, dist, flag,
                             st));
         std::vector<int> f2(nq);
         KCK(cudaMemcpyAsync(f2.data(), flag, sizeof(int) * nq, cudaMemcpyDeviceToHost, st));
@@ -414,7 +457,10 @@ int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist
             if (f2[k]) still.push_back(bad[k]);
         bad.swap(still);
     }
-    if (stats) stats->rows_unverified = (int) bad.size();
+    if (stats) {
+        stats->rows_unverified = (int) bad.size();
+        stats->s_rescans = secs() - s_first;
+    }
 #undef KCK
     cudaFree(Xf);
     cudaFree(cd);

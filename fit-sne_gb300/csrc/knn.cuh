@@ -20,6 +20,10 @@ namespace fitsne {
 struct KnnStats {
     int rows_rescanned = 0;    // rows that failed verification in the first pass
     int rows_unverified = 0;   // rows still unverified after the rescans (exact ties)
+    bool tensor_cores = false; // first pass ran on the tcgen05 kernel (knn_tc.cu)
+    double s_candidates = 0;   // host-clock seconds: first-pass candidates (tensor-core path)
+    double s_first_pass = 0;   // first pass including the re-rank
+    double s_rescans = 0;      // rescans of the unverified rows
 };
 
 // Xd: N x D FP64 (device).  Writes idx[N*K] and dist[N*K] (device, FP64 non-squared,

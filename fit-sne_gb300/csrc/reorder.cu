@@ -57,20 +57,66 @@ __global__ void k_perm_len(const uint32_t *__restrict__ row, const uint32_t *__r
     }
 }
 
+// Rows up to kSortRow entries are also sorted by (new) column index, so that the
+// attraction pass gathers neighbours in index order (adjacent lanes, adjacent lines).
+constexpr int kSortRow = 256;
+
 template <typename T>
-__global__ void k_perm_csr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
-                           const T *__restrict__ val, const uint32_t *__restrict__ order,
-                           const uint32_t *__restrict__ inv, const uint32_t *__restrict__ row_new, int N,
-                           uint32_t *__restrict__ col_new, T *__restrict__ val_new) {
-    const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(256) k_perm_csr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                                                  const T *__restrict__ val, const uint32_t *__restrict__ order,
+                                                  const uint32_t *__restrict__ inv,
+                                                  const uint32_t *__restrict__ row_new, int N,
+                                                  uint32_t *__restrict__ col_new, T *__restrict__ val_new) {
+    __shared__ uint32_t sc[8][kSortRow];
+    __shared__ T sv[8][kSortRow];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int k = gw; k < N; k += nw) {
         const uint32_t c = order[k];
         const uint32_t a = row[c], b = row[c + 1], o = row_new[k];
-        for (uint32_t e = a + lane; e < b; e += 32) {
-            col_new[o + (e - a)] = inv[col[e]];
-            val_new[o + (e - a)] = val[e];
+        const int len = (int) (b - a);
+        if (len > 1 && len <= kSortRow) {
+            int p2 = 2;
+            while (p2 < len) p2 <<= 1;
+            for (int i = lane; i < p2; i += 32) {
+                if (i < len) {
+                    sc[w][i] = inv[col[a + i]];
+                    sv[w][i] = val[a + i];
+                } else {
+                    sc[w][i] = 0xffffffffu;
+                    sv[w][i] = T(0);
+                }
+            }
+            __syncwarp();
+            for (int kk = 2; kk <= p2; kk <<= 1)
+                for (int j = kk >> 1; j > 0; j >>= 1) {
+                    for (int i = lane; i < p2; i += 32) {
+                        const int q = i ^ j;
+                        if (q > i) {
+                            const bool up = (i & kk) == 0;
+                            const uint32_t x = sc[w][i], y = sc[w][q];
+                            if ((x > y) == up) {
+                                sc[w][i] = y;
+                                sc[w][q] = x;
+                                const T t = sv[w][i];
+                                sv[w][i] = sv[w][q];
+                                sv[w][q] = t;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            for (int i = lane; i < len; i += 32) {
+                col_new[o + i] = sc[w][i];
+                val_new[o + i] = sv[w][i];
+            }
+            __syncwarp();
+        } else {
+            for (uint32_t e = a + lane; e < b; e += 32) {
+                col_new[o + (e - a)] = inv[col[e]];
+                val_new[o + (e - a)] = val[e];
+            }
         }
     }
 }

@@ -58,3 +58,47 @@ def test_kl_matches_reference(gpu_lib, golden, bits, name, yk, df):
         gpu_lib.set_precision(32)
     ref = float(golden[name + "_KL"])
     assert abs(c - ref) / abs(ref) < (1e-5 if bits == 32 else 1e-10)
+
+
+def _box_geometry(Y, min_int=50, ipi=1.0):
+    """Box count and width of the 2-D grid (the reference's rule, nbodyfft.cpp / tsne.cpp:1039-1060)."""
+    allowed = [25, 36, 50, 55, 60, 65, 70, 75, 80, 85, 90, 96, 100, 110, 120, 130, 140, 150, 175, 200]
+    v = Y.ravel()
+    mx, mn = v.max(), v[1:].min()
+    nb = int(max(min_int, (mx - mn) / ipi))
+    if nb < 200:
+        nb = next(a for a in allowed if a >= nb)
+    return mn, (mx - mn) / nb
+
+
+def test_fp32_box_index_agrees_with_fp64_on_a_box_edge(gpu_lib, golden):
+    """A point whose float box quotient rounds across an edge must still be interpolated
+    from the box the FP64 form (and the reference) picks: from the other box its
+    repulsion differs by the interpolation error, far above FP32 rounding."""
+    row, col, val = _P(golden)
+    Y = golden["Y2"].copy()
+    mn, bw = _box_geometry(Y)
+    i = int(np.argsort(np.abs(Y[:, 0] - np.median(Y[:, 0])))[0])  # an interior point
+    k = int((Y[i, 0] - mn) / bw)
+    found = False
+    for rel in np.geomspace(1e-9, 1e-6, 400):
+        x = mn + bw * (k + 1) * (1.0 - rel)
+        hi = np.float32(x)
+        x = float(hi) + float(np.float32(x - float(hi)))  # representable as a float pair
+        q32 = np.float32(np.float32(x - mn) * np.float32(1.0 / bw))
+        if int((x - mn) / bw) == k and int(q32) == k + 1:
+            found = True
+            break
+    assert found
+    Y[i, 0] = x
+    assert _box_geometry(Y) == (mn, bw)
+    out = {}
+    for bits in (32, 64):
+        gpu_lib.set_precision(bits)
+        try:
+            out[bits] = gpu_lib.fft_gradient(row, col, val, Y, 3, 1.0, 50, 1.0)
+        finally:
+            gpu_lib.set_precision(32)
+    g32, g64 = out[32][0], out[64][0]
+    assert np.linalg.norm(g32[i] - g64[i]) / np.linalg.norm(g64[i]) < 1e-4
+    assert rel_l2(g32, g64) < 1e-5

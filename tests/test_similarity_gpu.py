@@ -38,6 +38,24 @@ def test_knn_is_exact_against_bruteforce(gpu_lib, orc, N, D, K):
         assert set(idx[r][dist[r] < odist[r][-1]]) == set(oidx[r][odist[r] < odist[r][-1]])
 
 
+@pytest.mark.parametrize("N,D,K,spread", [(3001, 50, 91, 4.0), (4096, 64, 31, 0.3), (1500, 20, 100, 2.0)])
+def test_tensor_core_candidates_give_the_exact_lists(gpu_lib, monkeypatch, N, D, K, spread):
+    """The tcgen05 candidate search (BF16 hi/lo split) and the FP32 scan must end in the same
+    exact neighbour lists after the FP64 re-rank; tight clusters exercise the rescans."""
+    rng = np.random.default_rng(N + D)
+    centres = rng.standard_normal((8, D)) * spread
+    X = centres[rng.integers(0, 8, N)] + rng.standard_normal((N, D)) * 0.05
+    X = (X - X.mean(0)) / np.abs(X - X.mean(0)).max()
+    idx_tc, d_tc = gpu_lib.knn(X, K)
+    monkeypatch.setenv("FITSNE_KNN", "simt")
+    idx_s, d_s = gpu_lib.knn(X, K)
+    assert np.allclose(d_tc, d_s, rtol=0, atol=0)
+    diff = np.nonzero((idx_tc != idx_s).any(axis=1))[0]
+    for r in diff:  # only permutations within equal distances
+        for a in np.unique(d_tc[r]):
+            assert set(idx_tc[r][d_tc[r] == a]) == set(idx_s[r][d_s[r] == a])
+
+
 def test_calibration_matches_reference(gpu_lib, golden):
     X = golden["sim_X"]
     K = int(golden["sim_K"])
