@@ -429,23 +429,27 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 
 // ---------------------------------------------------------------------------------
 // CSR attraction fused with the optimiser step (tsne.cpp:1121-1155 and 479-531).
-// One warp per row; rows are strided over a fixed grid so that the mean of the new Y
-// reduces over few partials.
+//
+// Warps take groups of 32 consecutive rows from a work counter (so that the grid sweeps
+// one window of consecutive rows, whose neighbours share L1/L2 lines after the locality
+// renumbering, and every warp stays busy whatever the row lengths).  Lane j of a group
+// loads row j's pointers and Y with coalesced loads and, at the end, applies row j's update
+// (gains, momentum, clipping, double-float Y) — so per row only two memory round trips
+// remain: the CSR entries (prefetched into L2 while the previous row is processed) and the
+// neighbour Y gathers (L2-resident).  Within a row, lanes take kAttrUnroll edges each per
+// batch: all index / value loads first, then all gathers.
 template <typename T, int D>
-__global__ void __launch_bounds__(kBlock, 6) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+__global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
                                                  const T *__restrict__ val, const T *__restrict__ Yin,
                                                  T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
                                                  T *__restrict__ dC, const T *__restrict__ rep, int N,
                                                  UpdateParams p, RedScratch r) {
     typedef typename YL<T, D>::P P;
     __shared__ double sh[2 * 32];
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    // each block walks a contiguous range of rows, its warps on consecutive rows: after the
-    // locality renumbering those rows share most neighbours, so the Y gathers hit in L1
-    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    const int rows_pb = (N + gridDim.x - 1) / gridDim.x;
-    const int r0 = blockIdx.x * rows_pb;
-    const int r1 = min(N, r0 + rows_pb);
+    const int ngroups = (N + 31) >> 5;
+    const unsigned int nwarps = (gridDim.x * blockDim.x) >> 5;
     const double Zd = *r.z;
     const T zinv = T(1.0 / Zd);
     const T df = T(p.df);
@@ -459,94 +463,147 @@ __global__ void __launch_bounds__(kBlock, 6) k_attr(const uint32_t *__restrict__
         else
             msum[d] = 0.0;
     }
-    for (int i = r0 + wib; i < r1; i += wpb) {
-        P ci[D];
-        YL<T, D>::load(Yin, i, ci);
-        T a[D];
+    while (true) {
+        int g = 0;
+        if (lane == 0) g = (int) atomicAdd(r.count + 4, 1u);
+        g = __shfl_sync(full, g, 0);
+        if (g >= ngroups) break;
+        const int i0 = g << 5;
+        const int nr = min(32, N - i0);
+        const int my = i0 + lane;
+        const bool live = lane < nr;
+        const uint32_t rb = live ? row[my] : 0u;
+        const uint32_t re = live ? row[my + 1] : 0u;
+        P cmy[D];
+        if (live) {
+            YL<T, D>::load(Yin, my, cmy);
+        } else {
 #pragma unroll
-        for (int d = 0; d < D; ++d) a[d] = T(0);
-        const uint32_t e0 = row[i], e1 = row[i + 1];
-        // kAttrUnroll edges per lane per batch: all index / value loads first, then all
-        // neighbour gathers, so that each lane has several independent loads in flight
-        for (uint32_t base = e0; base < e1; base += 32 * kAttrUnroll) {
-            uint32_t j[kAttrUnroll];
-            T v[kAttrUnroll];
+            for (int d = 0; d < D; ++d) cmy[d] = P{};
+        }
+        T amy[D];
 #pragma unroll
-            for (int k = 0; k < kAttrUnroll; ++k) {
-                const uint32_t e = base + lane + 32 * k;
-                const bool ok = e < e1;
-                j[k] = ok ? __ldcs(col + e) : (uint32_t) i;
-                v[k] = ok ? __ldcs(val + e) : T(0);
-            }
-            P cj[kAttrUnroll][D];
-#pragma unroll
-            for (int k = 0; k < kAttrUnroll; ++k) YL<T, D>::load(Yin, (int) j[k], cj[k]);
-#pragma unroll
-            for (int k = 0; k < kAttrUnroll; ++k) {
-                T dx[D];
-                T d2 = T(0);
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    dx[d] = pdiff(ci[d], cj[k][d]);
-                    d2 += dx[d] * dx[d];
+        for (int d = 0; d < D; ++d) amy[d] = T(0);
+        for (int k = 0; k < nr; ++k) {
+            const uint32_t e0 = __shfl_sync(full, rb, k), e1 = __shfl_sync(full, re, k);
+            if (k + 1 < nr) {
+                // the next row's CSR lines into L2 (lanes 0-15 columns, 16-31 values)
+                const uint32_t f0 = __shfl_sync(full, rb, k + 1), f1 = __shfl_sync(full, re, k + 1);
+                if (f1 > f0) {
+                    const char *lo = lane < 16 ? reinterpret_cast<const char *>(col + f0)
+                                               : reinterpret_cast<const char *>(val + f0);
+                    const char *hi = lane < 16 ? reinterpret_cast<const char *>(col + f1)
+                                               : reinterpret_cast<const char *>(val + f1);
+                    const uintptr_t l0 = reinterpret_cast<uintptr_t>(lo) & ~(uintptr_t) 127;
+                    for (uintptr_t a = l0 + (uintptr_t) (lane & 15) * 128; a < reinterpret_cast<uintptr_t>(hi);
+                         a += 16 * 128)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
                 }
-                const T q = df1 ? T(1) / (T(1) + d2) : T(1) / (T(1) + d2 / df);
-                const T vq = v[k] * q;
+            }
+            const int i = i0 + k;
+            P ci[D];
 #pragma unroll
-                for (int d = 0; d < D; ++d) a[d] += vq * dx[d];
+            for (int d = 0; d < D; ++d) {
+                if constexpr (sizeof(T) == 4)
+                    ci[d] = {__shfl_sync(full, cmy[d].hi, k), __shfl_sync(full, cmy[d].lo, k)};
+                else
+                    ci[d] = __shfl_sync(full, cmy[d], k);
+            }
+            T a[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) a[d] = T(0);
+            for (uint32_t base = e0; base < e1; base += 32 * kAttrUnroll) {
+                uint32_t j[kAttrUnroll];
+                T v[kAttrUnroll];
+#pragma unroll
+                for (int u = 0; u < kAttrUnroll; ++u) {
+                    const uint32_t e = base + lane + 32 * u;
+                    const bool ok = e < e1;
+                    j[u] = ok ? __ldcs(col + e) : (uint32_t) i;
+                    v[u] = ok ? __ldcs(val + e) : T(0);
+                }
+                P cj[kAttrUnroll][D];
+#pragma unroll
+                for (int u = 0; u < kAttrUnroll; ++u) YL<T, D>::load(Yin, (int) j[u], cj[u]);
+#pragma unroll
+                for (int u = 0; u < kAttrUnroll; ++u) {
+                    T dx[D];
+                    T d2 = T(0);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        dx[d] = pdiff(ci[d], cj[u][d]);
+                        d2 += dx[d] * dx[d];
+                    }
+                    const T q = df1 ? T(1) / (T(1) + d2) : T(1) / (T(1) + d2 / df);
+                    const T vq = v[u] * q;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) a[d] += vq * dx[d];
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                for (int o = 16; o; o >>= 1) a[d] += __shfl_xor_sync(full, a[d], o);
+                if (lane == k) amy[d] = a[d];
             }
         }
+        if (!live) continue;
+        // ---- row `my`: gradient and update ----
+        T gr[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d)
-            for (int o = 16; o; o >>= 1) a[d] += __shfl_xor_sync(0xffffffffu, a[d], o);
-        if (lane == 0) {
-            T g[D];
+        for (int d = 0; d < D; ++d) gr[d] = exag * amy[d] - rep[(size_t) my * D + d] * zinv;
+        if (p.mode == 0) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) g[d] = exag * a[d] - rep[(size_t) i * D + d] * zinv;
-            if (p.mode == 0) {
+            for (int d = 0; d < D; ++d) dC[(size_t) my * D + d] = gr[d];
+            continue;
+        }
+        P cn[D];
+        if (p.use_gains) {
+            T u[D];
+            T nrm2 = T(0);
 #pragma unroll
-                for (int d = 0; d < D; ++d) dC[(size_t) i * D + d] = g[d];
-            } else {
-                P cn[D];
-                if (p.use_gains) {
-                    T u[D];
-                    T nrm2 = T(0);
+            for (int d = 0; d < D; ++d) {
+                T gn = gains[(size_t) my * D + d];
+                const T uo = uY[(size_t) my * D + d];
+                gn = (sgn(gr[d]) != sgn(uo)) ? (gn + T(0.2)) : (gn * T(0.8));
+                if (gn < T(0.01)) gn = T(0.01);
+                gains[(size_t) my * D + d] = gn;
+                u[d] = T(p.momentum) * uo - T(p.learning_rate) * gn * gr[d];
+                nrm2 += u[d] * u[d];
+            }
+            if (p.max_step_norm > 0) {
+                const T step = sqrt(nrm2);
+                if (step > T(p.max_step_norm)) {
+                    const T sc = T(p.max_step_norm) / step;
 #pragma unroll
-                    for (int d = 0; d < D; ++d) {
-                        T gn = gains[(size_t) i * D + d];
-                        const T uo = uY[(size_t) i * D + d];
-                        gn = (sgn(g[d]) != sgn(uo)) ? (gn + T(0.2)) : (gn * T(0.8));
-                        if (gn < T(0.01)) gn = T(0.01);
-                        gains[(size_t) i * D + d] = gn;
-                        u[d] = T(p.momentum) * uo - T(p.learning_rate) * gn * g[d];
-                        nrm2 += u[d] * u[d];
-                    }
-                    if (p.max_step_norm > 0) {
-                        const T step = sqrt(nrm2);
-                        if (step > T(p.max_step_norm)) {
-                            const T sc = T(p.max_step_norm) / step;
-#pragma unroll
-                            for (int d = 0; d < D; ++d) u[d] *= sc;
-                        }
-                    }
-#pragma unroll
-                    for (int d = 0; d < D; ++d) {
-                        uY[(size_t) i * D + d] = u[d];
-                        cn[d] = padd(ci[d], u[d]);
-                    }
-                } else {
-#pragma unroll
-                    for (int d = 0; d < D; ++d) cn[d] = padd(ci[d], -g[d]);
-                }
-                YL<T, D>::store(Yout, i, cn);
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    if constexpr (sizeof(T) == 4)
-                        msum[d] = df_add(msum[d], cn[d]);
-                    else
-                        msum[d] += cn[d];
+                    for (int d = 0; d < D; ++d) u[d] *= sc;
                 }
             }
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                uY[(size_t) my * D + d] = u[d];
+                cn[d] = padd(cmy[d], u[d]);
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < D; ++d) cn[d] = padd(cmy[d], -gr[d]);
+        }
+        YL<T, D>::store(Yout, my, cn);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            if constexpr (sizeof(T) == 4)
+                msum[d] = df_add(msum[d], cn[d]);
+            else
+                msum[d] += cn[d];
+        }
+    }
+    // the last warp out resets the work counter for the next launch (every warp's last
+    // counter increment is ordered before its exit increment by the fence)
+    if (lane == 0) {
+        __threadfence();
+        const unsigned int out = atomicAdd(r.count + 5, 1u);
+        if (out == nwarps - 1) {
+            atomicExch(r.count + 4, 0u);
+            atomicExch(r.count + 5, 0u);
         }
     }
     if (p.mode != 0) {
@@ -569,15 +626,13 @@ __global__ void __launch_bounds__(kBlock) k_kl(const uint32_t *__restrict__ row,
     typedef typename YL<T, D>::P P;
     __shared__ double sh[32];
     const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    const int rows_pb = (N + gridDim.x - 1) / gridDim.x;
-    const int r0 = blockIdx.x * rows_pb;
-    const int r1 = min(N, r0 + rows_pb);
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
     const T zinv = T(1.0 / *r.z);
     const T df = T(dfd);
     const T ex = T(exag);
     double acc[1] = {0.0};
-    for (int i = r0 + wib; i < r1; i += wpb) {
+    for (int i = gw; i < N; i += nw) {
         P ci[D];
         YL<T, D>::load(Y, i, ci);
         const uint32_t e1 = row[i + 1];
@@ -691,7 +746,20 @@ template <typename T>
 cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
                                T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
                                RedScratch r, cudaStream_t st) {
-    const int g = grid_for((long long) N * 32, kBlock, kRedGrid);
+    // one resident wave: the warps take row groups from a counter
+    static int wave[2] = {0, 0};
+    int &w = wave[D == 2 ? 1 : 0];
+    if (w == 0) {
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = (D == 2) ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, 2>, kBlock, 0)
+                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, 1>, kBlock, 0);
+        if (e != cudaSuccess) return e;
+        w = nsm * (per_sm > 0 ? per_sm : 1);
+        if (w > kMaxRedBlocks) w = kMaxRedBlocks;
+    }
+    const int g = grid_for(((long long) N + 31) / 32 * 32, kBlock, w);
     if (D == 2)
         k_attr<T, 2><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
     else

@@ -38,15 +38,22 @@ def test_knn_is_exact_against_bruteforce(gpu_lib, orc, N, D, K):
         assert set(idx[r][dist[r] < odist[r][-1]]) == set(oidx[r][odist[r] < odist[r][-1]])
 
 
-@pytest.mark.parametrize("N,D,K,spread", [(3001, 50, 91, 4.0), (4096, 64, 31, 0.3), (1500, 20, 100, 2.0)])
-def test_tensor_core_candidates_give_the_exact_lists(gpu_lib, monkeypatch, N, D, K, spread):
-    """The tcgen05 candidate search (BF16 hi/lo split) and the FP32 scan must end in the same
-    exact neighbour lists after the FP64 re-rank; tight clusters exercise the rescans."""
+@pytest.mark.parametrize("N,D,K,spread,path", [(3001, 50, 91, 4.0, "tcgen05"), (4096, 62, 31, 0.3, "tcgen05"),
+                                                (1500, 20, 100, 2.0, "FP32"), (2000, 63, 20, 1.0, "FP32"),
+                                                (70001, 50, 91, 3.0, "tcgen05")])
+def test_tensor_core_candidates_give_the_exact_lists(gpu_lib, monkeypatch, capfd, N, D, K, spread, path):
+    """The tcgen05 candidate search (BF16 hi/lo split, folded norms) and the FP32 scan must
+    end in the same exact neighbour lists after the FP64 re-rank; tight clusters exercise the
+    rescans, N = 70001 a ragged last tile of a multi-tile grid.  K + 29 > 120 candidates or
+    D > 62 take the FP32 scan."""
     rng = np.random.default_rng(N + D)
     centres = rng.standard_normal((8, D)) * spread
     X = centres[rng.integers(0, 8, N)] + rng.standard_normal((N, D)) * 0.05
     X = (X - X.mean(0)) / np.abs(X - X.mean(0)).max()
+    monkeypatch.setenv("FITSNE_TIMING", "1")
+    capfd.readouterr()
     idx_tc, d_tc = gpu_lib.knn(X, K)
+    assert path + " candidates" in capfd.readouterr().err
     monkeypatch.setenv("FITSNE_KNN", "simt")
     idx_s, d_s = gpu_lib.knn(X, K)
     assert np.allclose(d_tc, d_s, rtol=0, atol=0)
