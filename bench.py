@@ -8,22 +8,32 @@ weights, per-cluster std U(0.5, 2), centres N(0, 25 I), seed 42); perplexity 30,
 2-D, df = 1, learning rate N/12, nterms 3, min_num_intervals 50, intervals_per_integer 1.
 A *step* is one optimiser iteration after the early exaggeration (exaggeration 1,
 momentum 0.8): spread + FFT convolution + gather on the interpolation grid, attraction over
-the ~1.3e8 non-zeros of P, gains/momentum/clipping update, zero-mean.  Steps start from the
-same synthetic expanded embedding (10 clusters, centres N(0, 40^2 I), spread 6), which puts
-the grid at its late-run size (200 boxes per side).
+the ~1.56e8 non-zeros of P, gains/momentum/clipping update, zero-mean.
 
 gb300 arm: P is built on the GPU from the data (exact kNN, calibration, symmetrisation) and
-stays resident; W untimed steps, then K steps timed with CUDA events on the library's stream.
+stays resident; the reference schedule runs untimed from a random start to iteration 300
+(early exaggeration until 250), then W untimed steps, then K steps timed with CUDA events
+on the library's stream (the grid grows from ~50 to ~70 boxes per side over those steps).
 `e2e` runs the whole pipeline (fitsne_run: data on the host -> embedding on the host, 1000
 iterations of the reference schedule) and reports iterations/s over that wall time.
 The FP64 form of the same kernels is timed on the same steps (`plain_fp64`) and the FP32
 gradient is compared with the FP64 one at the starting state (`grad_rel_l2_vs_fp64`).
 
-reference arm: the reference's CPU path (the C restatement in oracle/, the reference tree is
-not on the GPU machine) on all host cores, on the same step definition; P for that arm is built
-on the CPU from random within-cluster neighbour lists of the same size (K = 90 per row,
-symmetrised by the restated symmetrizeMatrix): the exact kNN of 1M points on the CPU takes
-hours.  The number of timed CPU steps is capped so that the arm ends within a few minutes.
+reference arm (and the cpu_baseline leg of the gb300 arm, same inputs): the reference's CPU
+path (the C restatement in oracle/, the reference tree is not on the GPU machine) on all host
+cores, on the same step definition; P for that arm is built on the CPU from random
+within-cluster neighbour lists of the same size (K = 90 per row, symmetrised by the restated
+symmetrizeMatrix): the exact kNN of 1M points on the CPU takes hours.  Y is a synthetic
+post-exaggeration embedding of the same clusters whose grid (60 boxes per side) is the middle
+of the GPU's timed steps.  The number of timed CPU steps is capped so that the arm ends
+within a few minutes.
+
+    python bench.py --stage similarities [--n N]
+
+times the input-similarity stage alone on the GPU (exact kNN with the tcgen05 candidate
+search, perplexity calibration, symmetrisation) on the same mixture, K = 91 with self, and
+reports the kNN candidate search against the tensor-core roofline (2 N^2 D flops, D = 50
+unpadded, against the measured bf16 peak).
 """
 from __future__ import annotations
 
@@ -49,6 +59,7 @@ SCHEDULE = dict(max_iter=1000, stop_lying_iter=250, mom_switch_iter=250, momentu
                 early_exag_coeff=12.0, max_step_norm=5.0)
 STEP_IT0 = 300  # steps are iterations of the post-exaggeration phase
 HBM_FALLBACK_GBS = 6800.0
+BF16_FALLBACK_TFLOPS = 1900.0
 
 
 def mixture(N, D=D_IN, seed=42):
@@ -64,10 +75,12 @@ def mixture(N, D=D_IN, seed=42):
 
 
 def expanded_state(labels, seed=7):
-    """Synthetic post-exaggeration embedding of the same clusters (extent ~ +-100)."""
+    """Synthetic post-exaggeration embedding of the same clusters: centres N(0, 12^2 I),
+    spread 2.5, range ~59 at N = 1M, i.e. a 60-box grid, the middle of the 50 -> 70 boxes that
+    the GPU's timed steps (iterations 305-605 of the real schedule) pass through."""
     rng = np.random.default_rng(seed)
-    centres = rng.standard_normal((10, 2)) * 40.0
-    Y = centres[labels] + rng.standard_normal((len(labels), 2)) * 6.0
+    centres = rng.standard_normal((10, 2)) * 12.0
+    Y = centres[labels] + rng.standard_normal((len(labels), 2)) * 2.5
     return Y - Y.mean(0)
 
 
@@ -160,6 +173,21 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return HBM_FALLBACK_GBS, "fallback"
+
+
+def bf16_peak():
+    """Dense bf16 TFLOP/s of this machine's GB300 (burst figure: the kNN kernel runs alone)."""
+    try:
+        p = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return BF16_FALLBACK_TFLOPS, "fallback"
+
+
+# DRAM bytes (read + write) of one attraction launch / its algorithmic bytes, from an ncu
+# capture of k_attr at N = 200,000 (nnz = 30,344,422): 256,773,632 / 257,955,380.  Traffic
+# grows with nnz (the CSR stream dominates), so the ratio carries to N = 1M.
+ATTR_TRAFFIC_RATIO = 256773632 / 257955380
 
 
 def attraction_bytes(N, nnz):
@@ -282,11 +310,20 @@ def run_gb300(args, world, rank, local):
         Yout, costs = fitsne.run(X, Y0=Y0, perplexity=PERPLEXITY, learning_rate=N / 12.0, knn_algo=2, **SCHEDULE)
         e2e_s = reduce_max(time.perf_counter() - t2, world)
         iters = SCHEDULE["max_iter"]
+        # the plain FP64 form end to end (same kNN, FP64 iterations)
+        fitsne.set_precision(64)
+        try:
+            t3 = time.perf_counter()
+            _, costs64 = fitsne.run(X, Y0=Y0, perplexity=PERPLEXITY, learning_rate=N / 12.0, knn_algo=2, **SCHEDULE)
+            e2e64_s = reduce_max(time.perf_counter() - t3, world)
+        finally:
+            fitsne.set_precision(32)
         e2e = {"value": world * iters / e2e_s, "unit": "iters/s", "seconds": e2e_s,
                "h2d_bytes_per_step": int((X.nbytes + Y0.nbytes) / iters),
                "d2h_bytes_per_step": int((Yout.nbytes + 16 * iters + 8 * (iters // 50)) / iters),
                "note": "whole fitsne_run (similarities + %d iterations), bytes averaged per iteration" % iters,
-               "final_kl": float(costs[-1])}
+               "final_kl": float(costs[-1]),
+               "plain_fp64": {"seconds": e2e64_s, "final_kl": float(costs64[-1]), "speedup": e2e64_s / e2e_s}}
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -308,7 +345,8 @@ def run_gb300(args, world, rank, local):
             "data": "synthetic (seeded Gaussian mixture)", "config": config(args, "GB300 sm_103a kernels"),
             "roofline": {"bound": "hbm", "kernel": "attraction + update (k_attr)", "achieved": achieved,
                          "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "bytes_per_launch": abytes, "ms_per_launch": attr_ms},
+                         "traffic": ATTR_TRAFFIC_RATIO * abytes, "bytes_per_launch": abytes,
+                         "ms_per_launch": attr_ms},
             "stage_ms": {"centre_minmax": st[0], "spread": st[1], "fft_conv": st[2], "gather": st[3],
                          "attraction_update": st[4], "iteration": st[5], "boxes_per_dim": st[6], "fft_len": st[7]},
             "nnz": nnz, "wall_ms_per_step": 1e3 * wall / args.steps, "setup_s": setup_s,
@@ -316,6 +354,50 @@ def run_gb300(args, world, rank, local):
             "plain_fp64": {"value": fp64_value, "unit": "iters/s", "steps": k64, "speedup": value / fp64_value},
             "grad_rel_l2_vs_fp64": grad_rel, "Z": z32,
             "gpu_launches": int(st[9]), "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e}
+    print(json.dumps(line))
+    return 0
+
+
+def run_similarities(args, world, rank):
+    """The input-similarity stage alone (kNN + calibration + symmetrisation) on the GPU."""
+    if rank != 0:
+        return 0
+    import fitsne
+    X, _, _ = mixture(args.n)
+    Xn = X - X.mean(0)
+    Xn /= np.abs(Xn).max()
+    os.environ["FITSNE_TIMING"] = "1"
+    times = []
+    for rep in range(1 + args.warmup // 3):
+        with tempfile.TemporaryFile(mode="w+") as log:
+            fd = sys.stderr.fileno()
+            saved = os.dup(fd)
+            os.dup2(log.fileno(), fd)
+            try:
+                t0 = time.perf_counter()
+                row, col, val = fitsne.gaussian_perplexity(Xn, PERPLEXITY, K_NEIGH)
+                t1 = time.perf_counter()
+                fitsne.symmetrize(row, col, val, args.n)
+                t2 = time.perf_counter()
+            finally:
+                os.dup2(saved, fd)
+                os.close(saved)
+            log.seek(0)
+            text = log.read()
+        times.append((t1 - t0, t2 - t1, text))
+    knn_s, sym_s, text = times[-1]
+    cand_s = float(text.split("candidates ")[1].split(" s")[0]) if "candidates " in text else None
+    peak, kind = bf16_peak()
+    flops = 2.0 * args.n * args.n * D_IN
+    line = {"metric": "similarity stage seconds (kNN K=91 + calibration; symmetrisation)", "value": knn_s + sym_s,
+            "unit": "s", "n_gpus": 1, "higher_is_better": False, "data": "synthetic (seeded Gaussian mixture)",
+            "config": {"workload": "N=%d x D=50 Gaussian mixture, perplexity 30, K=90" % args.n},
+            "knn_and_calibration_s": knn_s, "symmetrisation_s": sym_s, "stage_log": text.strip().splitlines(),
+            "roofline": {"bound": "tensor", "kernel": "tcgen05 kNN candidate search (k_knn_tc)",
+                         "achieved": flops / cand_s / 1e12 if cand_s else None, "peak": peak, "peak_kind": kind,
+                         "unit": "TFLOP/s", "frac": flops / cand_s / 1e12 / peak if cand_s else None,
+                         "flops": flops, "note": "2 N^2 D algorithmic flops (D = 50 unpadded) over the host-clock "
+                                                 "time of the candidate phase (BF16 planes + kernel)"}}
     print(json.dumps(line))
     return 0
 
@@ -330,6 +412,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--stage", default="iteration", choices=["iteration", "similarities"])
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
@@ -339,7 +422,12 @@ def main():
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    rc = run_reference(args, world, rank) if args.impl == "reference" else run_gb300(args, world, rank, local)
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank)
+    elif args.stage == "similarities":
+        rc = run_similarities(args, world, rank)
+    else:
+        rc = run_gb300(args, world, rank, local)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -9,6 +9,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kRedGrid = 1216;  // 152 SMs x 8 resident blocks of 256 threads
 constexpr int kAttrUnroll = 4;  // CSR edges per lane per batch in the attraction pass
+constexpr int kAttrGroup = 16;  // consecutive rows per work item of the attraction pass (<= 32)
 
 // ---------------------------------------------------------------------------------
 // storage layouts of Y
@@ -430,7 +431,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 // ---------------------------------------------------------------------------------
 // CSR attraction fused with the optimiser step (tsne.cpp:1121-1155 and 479-531).
 //
-// Warps take groups of 32 consecutive rows from a work counter (so that the grid sweeps
+// Warps take groups of kAttrGroup consecutive rows from a work counter (so that the grid sweeps
 // one window of consecutive rows, whose neighbours share L1/L2 lines after the locality
 // renumbering, and every warp stays busy whatever the row lengths).  Lane j of a group
 // loads row j's pointers and Y with coalesced loads and, at the end, applies row j's update
@@ -448,7 +449,7 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
     __shared__ double sh[2 * 32];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int ngroups = (N + 31) >> 5;
+    const int ngroups = (N + kAttrGroup - 1) / kAttrGroup;
     const unsigned int nwarps = (gridDim.x * blockDim.x) >> 5;
     const double Zd = *r.z;
     const T zinv = T(1.0 / Zd);
@@ -468,8 +469,8 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
         if (lane == 0) g = (int) atomicAdd(r.count + 4, 1u);
         g = __shfl_sync(full, g, 0);
         if (g >= ngroups) break;
-        const int i0 = g << 5;
-        const int nr = min(32, N - i0);
+        const int i0 = g * kAttrGroup;
+        const int nr = min(kAttrGroup, N - i0);
         const int my = i0 + lane;
         const bool live = lane < nr;
         const uint32_t rb = live ? row[my] : 0u;
