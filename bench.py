@@ -34,6 +34,12 @@ times the input-similarity stage alone on the GPU (exact kNN with the tcgen05 ca
 search, perplexity calibration, symmetrisation) on the same mixture, K = 91 with self, and
 reports the kNN candidate search against the tensor-core roofline (2 N^2 D flops, D = 50
 unpadded, against the measured bf16 peak).
+
+    python bench.py --stage batch [--jobs 64]
+
+runs the batched form (fitsne_batch_run: 64 embeddings, N log-uniform in [2,000, 50,000],
+D = 50 mixtures of 5-30 clusters, perplexity 10 / 30 / 50 cycled, 1000 iterations) and the
+same jobs one by one through fitsne_run, and reports the aggregate iterations/s.
 """
 from __future__ import annotations
 
@@ -402,6 +408,60 @@ def run_similarities(args, world, rank):
     return 0
 
 
+def batch_jobs(njobs=64, seed=5):
+    """Batched workload: N log-uniform in [2,000, 50,000], D = 50 Gaussian mixtures with
+    5-30 clusters (Dirichlet(2) weights, std U(0.5, 2), centres N(0, 25 I)), perplexity
+    10 / 30 / 50 cycled (K = 3 perplexity), learning rate max(200, N / 12)."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(njobs):
+        N = int(round(np.exp(rng.uniform(np.log(2000), np.log(50000)))))
+        k = int(rng.integers(5, 31))
+        w = rng.dirichlet(np.full(k, 2.0))
+        lab = np.repeat(np.arange(k), rng.multinomial(N, w))
+        c = rng.standard_normal((k, D_IN)) * 5.0
+        X = c[lab] + rng.standard_normal((N, D_IN)) * rng.uniform(0.5, 2.0, k)[lab, None]
+        jobs.append((X, (10.0, 30.0, 50.0)[j % 3], max(200.0, N / 12.0)))
+    return jobs
+
+
+def run_batch(args, world, rank):
+    """The batched form (fitsne_batch_run) against the same jobs run one by one."""
+    if rank != 0:
+        return 0
+    import fitsne
+    jobs = batch_jobs(args.jobs)
+    Xs = [j[0] for j in jobs]
+    perps = [j[1] for j in jobs]
+    lrs = [j[2] for j in jobs]
+    rng = np.random.default_rng(9)
+    Y0s = [rng.standard_normal((len(X), 2)) * 1e-4 for X in Xs]
+    iters = 1000
+    t0 = time.perf_counter()
+    Ys, costs, st = fitsne.batch_run(Xs, perps, learning_rates=lrs, Y0s=Y0s, max_iter=iters)
+    batch_s = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    single_kl = []
+    for X, p, lr, Y0 in zip(Xs, perps, lrs, Y0s):
+        _, c = fitsne.run(X, Y0=Y0, perplexity=p, learning_rate=lr, max_iter=iters, knn_algo=2)
+        single_kl.append(c[-1])
+    single_s = time.perf_counter() - t1
+    kl_dev = max(abs(c[-1] - k) / k for c, k in zip(costs, single_kl))
+    n = [len(X) for X in Xs]
+    line = {"metric": "batched t-SNE: aggregate iterations/s over %d independent embeddings" % len(jobs),
+            "value": len(jobs) * iters / batch_s, "unit": "iters/s", "n_gpus": 1, "higher_is_better": True,
+            "data": "synthetic (seeded Gaussian mixtures)",
+            "config": {"workload": "%d jobs, N log-uniform in [2000, 50000] (total %d points), D=50, 5-30 clusters, "
+                                   "perplexity 10/30/50 cycled, 2-D, df=1, %d iterations" % (len(jobs), sum(n), iters)},
+            "batch_seconds": batch_s, "similarity_seconds": st["similarity_s"], "iterate_seconds": st["iterate_s"],
+            "iterate_iters_per_s": len(jobs) * iters / st["iterate_s"], "graph_launches": st["graph_launches"],
+            "graph_captures": st["graph_captures"], "chunks_redone": st["chunks_redone"],
+            "one_by_one_seconds": single_s, "speedup_vs_one_by_one": single_s / batch_s,
+            "max_final_kl_rel_dev_vs_one_by_one": kl_dev}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -412,7 +472,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--stage", default="iteration", choices=["iteration", "similarities"])
+    ap.add_argument("--stage", default="iteration", choices=["iteration", "similarities", "batch"])
+    ap.add_argument("--jobs", type=int, default=64)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
@@ -426,6 +487,8 @@ def main():
         rc = run_reference(args, world, rank)
     elif args.stage == "similarities":
         rc = run_similarities(args, world, rank)
+    elif args.stage == "batch":
+        rc = run_batch(args, world, rank)
     else:
         rc = run_gb300(args, world, rank, local)
     if world > 1:

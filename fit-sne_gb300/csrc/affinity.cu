@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "affinity.cuh"
+#include "calib_mlp.cuh"
 #include "knn.cuh"
 #include "sort.cuh"
 
@@ -70,7 +71,7 @@ __global__ void k_scale(double *__restrict__ X, size_t n, const unsigned long lo
 // inside the loop before testing, so P corresponds to the beta of the last evaluation;
 // this helper reproduces that beta and writes the normalised row.
 __device__ double calibrate_row(const double *__restrict__ d, double *__restrict__ p, int K, double perplexity,
-                                double sigma) {
+                                double sigma, int *evals = nullptr) {
     double beta_eval;
     if (perplexity > 0) {
         double min_beta = -DBL_MAX, max_beta = DBL_MAX;
@@ -107,6 +108,7 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
             }
             iter++;
         }
+        if (evals) *evals = iter;
         // P of the reference is the row evaluated at beta_eval; the returned beta is the
         // updated one when the loop ran out of iterations (as in the reference)
         double sum_P = DBL_MIN;
@@ -129,17 +131,19 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
 
 __global__ void k_calibrate(const double *__restrict__ dist, int stride, int offset, double *__restrict__ P,
                             double *__restrict__ tmp, int nrows, int K, double perplexity, double sigma,
-                            const double *__restrict__ list, int list_len, double *__restrict__ beta_out) {
+                            const double *__restrict__ list, int list_len, double *__restrict__ beta_out,
+                            int *__restrict__ evals_out) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
     const double *d = dist + (size_t) r * stride + offset;
     double *p = P + (size_t) r * K;
     double beta;
+    int evals = 0;
     if (perplexity != 0) {
-        beta = calibrate_row(d, p, K, perplexity, sigma);
+        beta = calibrate_row(d, p, K, perplexity, sigma, &evals);
     } else {
         double *t = tmp + (size_t) r * K;
-        beta = calibrate_row(d, p, K, list[0], sigma);
+        beta = calibrate_row(d, p, K, list[0], sigma, &evals);
         for (int m = 1; m < list_len; ++m) {
             beta = calibrate_row(d, t, K, list[m], sigma);
             for (int i = 0; i < K; ++i) p[i] += t[i];
@@ -147,6 +151,7 @@ __global__ void k_calibrate(const double *__restrict__ dist, int stride, int off
         for (int i = 0; i < K; ++i) p[i] /= list_len;
     }
     if (beta_out) beta_out[r] = beta;
+    if (evals_out) evals_out[r] = evals;
 }
 
 __global__ void k_knn_to_csr(const uint32_t *__restrict__ idx, int N, int K, uint32_t *__restrict__ row,
@@ -357,8 +362,10 @@ int prepare_X(const double *X_host, int N, int D, bool normalize, double **Xd_ou
 
 int calibrate_rows(const double *dist, int stride, int offset, double *P, int nrows, int K, double perplexity,
                    double sigma, int list_len, const double *list_host, double *beta, cudaStream_t st,
-                   std::string &err) {
+                   std::string &err, std::vector<int> *iters) {
     double *list = nullptr, *tmp = nullptr;
+    int *evals = nullptr;
+    if (iters) ACK(cudaMalloc(&evals, sizeof(int) * (size_t) (nrows > 0 ? nrows : 1)));
     if (perplexity == 0) {
         if (list_len < 1 || !list_host) {
             err = "perplexity 0 needs a perplexity list";
@@ -369,11 +376,16 @@ int calibrate_rows(const double *dist, int stride, int offset, double *P, int nr
         ACK(cudaMalloc(&tmp, sizeof(double) * (size_t) nrows * K));
     }
     k_calibrate<<<(nrows + 127) / 128, 128, 0, st>>>(dist, stride, offset, P, tmp, nrows, K, perplexity, sigma, list,
-                                                      list_len, beta);
+                                                      list_len, beta, evals);
     ACK(cudaGetLastError());
+    if (iters) {
+        iters->resize(nrows);
+        ACK(cudaMemcpyAsync(iters->data(), evals, sizeof(int) * (size_t) nrows, cudaMemcpyDeviceToHost, st));
+    }
     ACK(cudaStreamSynchronize(st));
     cudaFree(list);
     cudaFree(tmp);
+    cudaFree(evals);
     return 0;
 }
 
@@ -415,8 +427,31 @@ int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double per
     k_knn_to_csr<<<4096, 256, 0, st>>>(idx, N, K, P.row, P.col);
     ACK(cudaGetLastError());
     const double t1 = now_s();
-    rc = calibrate_rows(dist, K + 1, 1, P.val, N, K, perplexity, sigma, list_len, list_host, nullptr, st, err);
-    if (tm) std::fprintf(stderr, "[fitsne] calibration: %.3f s\n", now_s() - t1);
+    if (calibration_mode() == 1 && perplexity > 0 && list_len == 0) {
+        MlpStats ms;
+        rc = calibrate_rows_learned(dist, K + 1, 1, P.val, N, K, perplexity, st, &ms, err);
+        if (!rc) store_calibration_stats(ms);
+        if (tm && !rc)
+            std::fprintf(stderr,
+                         "[fitsne] calibration (learned warm start): %.3f s; %d harvested rows, %.1f evaluations "
+                         "per row; %d training steps, loss %.3g -> %.3g; %d predicted rows, %.2f evaluations per "
+                         "row, %d with bisection steps\n",
+                         now_s() - t1, ms.rows_harvest, ms.iters_plain, ms.train_steps, ms.loss_first, ms.loss_last,
+                         ms.rows - ms.rows_harvest, ms.iters_warm, ms.rows_fallback);
+    } else {
+        std::vector<int> evals;
+        rc = calibrate_rows(dist, K + 1, 1, P.val, N, K, perplexity, sigma, list_len, list_host, nullptr, st, err,
+                            &evals);
+        if (!rc) {
+            MlpStats ms;
+            ms.rows = ms.rows_harvest = N;
+            double s = 0;
+            for (int v : evals) s += v;
+            ms.iters_plain = N ? s / N : 0;
+            store_calibration_stats(ms);
+        }
+        if (tm) std::fprintf(stderr, "[fitsne] calibration: %.3f s\n", now_s() - t1);
+    }
     cudaFree(idx);
     cudaFree(dist);
     if (rc) {

@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -38,10 +39,11 @@ void free_csr(DevCSR &P);
 int prepare_X(const double *X_host, int N, int D, bool normalize, double **Xd, cudaStream_t st, std::string &err);
 
 // Row-wise calibration of K distances per row (row r at dist + r*stride + offset).
-// P receives nrows x K similarities, beta (may be null) the precisions.
+// P receives nrows x K similarities, beta (may be null) the precisions, iters (may be null)
+// the number of entropy evaluations of each row (the first perplexity of a list).
 int calibrate_rows(const double *dist, int stride, int offset, double *P, int nrows, int K, double perplexity,
                    double sigma, int list_len, const double *list_host, double *beta, cudaStream_t st,
-                   std::string &err);
+                   std::string &err, std::vector<int> *iters = nullptr);
 
 // kNN + calibration into fixed-length rows (row n = n*K).  Xd on the device.
 int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double perplexity, double sigma, int list_len,

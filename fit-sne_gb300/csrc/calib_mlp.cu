@@ -1,0 +1,546 @@
+// Learned warm start of the perplexity calibration (see calib_mlp.cuh).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "affinity.cuh"
+#include "calib_mlp.cuh"
+
+namespace fitsne {
+namespace {
+
+constexpr int H = kMlpHidden;
+constexpr int kSPB = 8;          // samples per block in the gradient kernel
+constexpr int kBatch = 256;      // minibatch
+constexpr int kGraphSteps = 25;  // optimiser steps per captured graph
+constexpr float kLr = 2e-3f;     // Adam step size
+constexpr int kH2 = H + 1;       // padded row stride of W2 in shared memory
+
+struct Offs {
+    int w1, b1, w2, b2, w3, b3, n;
+};
+__host__ __device__ inline Offs offs(int K) {
+    Offs o;
+    o.w1 = 0;
+    o.b1 = H * K;
+    o.w2 = o.b1 + H;
+    o.b2 = o.w2 + H * H;
+    o.w3 = o.b2 + H;
+    o.b3 = o.w3 + H;
+    o.n = o.b3 + 1;
+    return o;
+}
+
+__host__ __device__ inline int odd_stride(int K) { return K | 1; }  // conflict-free row reads
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// ---- features: x = d / mean(d), scale = mean(d); target = log(beta * mean(d)) --------------
+__global__ void k_features(const double *__restrict__ dist, int stride, int offset, int nrows, int K,
+                           const double *__restrict__ beta, float *__restrict__ x, float *__restrict__ scale,
+                           float *__restrict__ target) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+        const double *d = dist + (size_t) r * stride + offset;
+        double s = 0.0;
+        for (int j = 0; j < K; ++j) s += d[j];
+        s /= K;
+        const bool ok = s > 0.0 && isfinite(s);
+        const double inv = ok ? 1.0 / s : 0.0;
+        for (int j = 0; j < K; ++j) x[(size_t) r * K + j] = (float) (d[j] * inv);
+        scale[r] = ok ? (float) s : 0.f;
+        if (target) target[r] = (ok && beta[r] > 0.0) ? (float) log(beta[r] * s) : 0.f;
+    }
+}
+
+__device__ __forceinline__ unsigned mix32(unsigned a, unsigned b) {
+    unsigned h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return h;
+}
+
+// ---- forward + backward of one minibatch ----------------------------------------------------
+// 64 threads (one per hidden unit) per block, kSPB samples per block, gradients accumulated
+// per block in shared memory and added to `grad` (FP32 atomics).  Standardised target
+// (target - mu) / sd; loss = mean squared error over the batch.  With step == nullptr the
+// batch is rows 0 .. batch-1 in order, else rows drawn by a hash of (step, position).
+__global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params, int K, const float *__restrict__ x,
+                                                 const float *__restrict__ target, int nrows, int batch, float mu,
+                                                 float inv_sd, const unsigned *__restrict__ step,
+                                                 float *__restrict__ grad, double *__restrict__ loss) {
+    extern __shared__ float sm[];
+    const int KP = odd_stride(K);
+    float *W1 = sm;
+    float *W2 = W1 + H * KP;
+    float *gW1 = W2 + H * kH2;
+    float *gW2 = gW1 + H * KP;
+    float *xs = gW2 + H * kH2;
+    float *h1 = xs + KP;
+    float *dh2 = h1 + H;
+    float *red = dh2 + H;
+    const unsigned full = 0xffffffffu;
+    const int u = threadIdx.x;
+    const Offs o = offs(K);
+    for (int e = u; e < H * K; e += H) {
+        const int r = e / K, c = e % K;
+        W1[r * KP + c] = params[o.w1 + e];
+        gW1[r * KP + c] = 0.f;
+    }
+    for (int e = u; e < H * H; e += H) {
+        const int r = e / H, c = e % H;
+        W2[r * kH2 + c] = params[o.w2 + e];
+        gW2[r * kH2 + c] = 0.f;
+    }
+    const float b1 = params[o.b1 + u], b2 = params[o.b2 + u], w3 = params[o.w3 + u], b3 = params[o.b3];
+    float gb1 = 0.f, gb2 = 0.f, gw3 = 0.f, gb3 = 0.f;
+    double lsum = 0.0;
+    const unsigned stp = step ? *step : 0u;
+    __syncthreads();
+    for (int q = 0; q < kSPB; ++q) {
+        const int pos = blockIdx.x * kSPB + q;
+        if (pos >= batch) break;  // uniform over the block
+        const int row = step ? (int) (mix32(stp, (unsigned) pos) % (unsigned) nrows) : pos;
+        for (int j = u; j < K; j += H) xs[j] = x[(size_t) row * K + j];
+        __syncthreads();
+        float a1 = b1;
+        for (int j = 0; j < K; ++j) a1 = fmaf(W1[u * KP + j], xs[j], a1);
+        h1[u] = a1 > 0.f ? a1 : 0.f;
+        __syncthreads();
+        float a2 = b2;
+        for (int k = 0; k < H; ++k) a2 = fmaf(W2[u * kH2 + k], h1[k], a2);
+        const float r2 = a2 > 0.f ? a2 : 0.f;
+        float p = w3 * r2;
+        for (int off = 16; off; off >>= 1) p += __shfl_xor_sync(full, p, off);
+        if ((u & 31) == 0) red[u >> 5] = p;
+        __syncthreads();
+        const float out = red[0] + red[1] + b3;
+        const float err = out - (target[row] - mu) * inv_sd;
+        if (u == 0) lsum += (double) err * err;
+        const float dout = 2.f * err / (float) batch;
+        gw3 = fmaf(dout, r2, gw3);
+        if (u == 0) gb3 += dout;
+        const float d2 = a2 > 0.f ? dout * w3 : 0.f;
+        dh2[u] = d2;
+        gb2 += d2;
+        for (int k = 0; k < H; ++k) gW2[u * kH2 + k] = fmaf(d2, h1[k], gW2[u * kH2 + k]);
+        __syncthreads();
+        float s = 0.f;
+        for (int v = 0; v < H; ++v) s = fmaf(dh2[v], W2[v * kH2 + u], s);
+        const float d1 = a1 > 0.f ? s : 0.f;
+        gb1 += d1;
+        for (int j = 0; j < K; ++j) gW1[u * KP + j] = fmaf(d1, xs[j], gW1[u * KP + j]);
+        __syncthreads();
+    }
+    for (int e = u; e < H * K; e += H) atomicAdd(&grad[o.w1 + e], gW1[(e / K) * KP + e % K]);
+    for (int e = u; e < H * H; e += H) atomicAdd(&grad[o.w2 + e], gW2[(e / H) * kH2 + e % H]);
+    atomicAdd(&grad[o.b1 + u], gb1);
+    atomicAdd(&grad[o.b2 + u], gb2);
+    atomicAdd(&grad[o.w3 + u], gw3);
+    if (u == 0) {
+        atomicAdd(&grad[o.b3], gb3);
+        atomicAdd(loss, lsum);
+    }
+}
+
+size_t grad_smem(int K) {
+    const int KP = odd_stride(K);
+    return sizeof(float) * (2 * (size_t) H * KP + 2 * (size_t) H * kH2 + KP + 2 * H + 2);
+}
+
+// ---- Adam (one block): update, zero the gradient, record the loss, advance the step --------
+__global__ void __launch_bounds__(1024) k_adam(float *__restrict__ params, float *__restrict__ grad,
+                                               float *__restrict__ m, float *__restrict__ v, int n,
+                                               unsigned *__restrict__ step, double *__restrict__ loss_acc,
+                                               float *__restrict__ loss_hist, int batch) {
+    const unsigned t = *step + 1u;
+    const float c1 = 1.f - powf(0.9f, (float) t), c2 = 1.f - powf(0.999f, (float) t);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float g = grad[i];
+        const float mi = 0.9f * m[i] + 0.1f * g;
+        const float vi = 0.999f * v[i] + 0.001f * g * g;
+        m[i] = mi;
+        v[i] = vi;
+        params[i] -= kLr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
+        grad[i] = 0.f;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        loss_hist[t - 1] = (float) (*loss_acc / batch);
+        *loss_acc = 0.0;
+        *step = t;
+    }
+}
+
+// ---- inference with BF16-rounded weights (FP32 accumulation) --------------------------------
+__global__ void __launch_bounds__(H) k_mlp_infer(const float *__restrict__ params, int K, const float *__restrict__ x,
+                                                  const float *__restrict__ scale, int nrows, float mu, float sd,
+                                                  double *__restrict__ beta_hat) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int KP = odd_stride(K);
+    __nv_bfloat16 *W1 = reinterpret_cast<__nv_bfloat16 *>(smraw);
+    __nv_bfloat16 *W2 = W1 + H * KP;
+    float *xs = reinterpret_cast<float *>(smraw + (((size_t) H * KP + (size_t) H * kH2) * 2 + 15) / 16 * 16);
+    float *h1 = xs + KP;
+    float *red = h1 + H;
+    const unsigned full = 0xffffffffu;
+    const int u = threadIdx.x;
+    const Offs o = offs(K);
+    for (int e = u; e < H * K; e += H) W1[(e / K) * KP + e % K] = __float2bfloat16(params[o.w1 + e]);
+    for (int e = u; e < H * H; e += H) W2[(e / H) * kH2 + e % H] = __float2bfloat16(params[o.w2 + e]);
+    const float b1 = params[o.b1 + u], b2 = params[o.b2 + u], w3 = __bfloat162float(__float2bfloat16(params[o.w3 + u]));
+    const float b3 = params[o.b3];
+    __syncthreads();
+    for (int r = blockIdx.x; r < nrows; r += gridDim.x) {
+        for (int j = u; j < K; j += H) xs[j] = x[(size_t) r * K + j];
+        __syncthreads();
+        float a1 = b1;
+        for (int j = 0; j < K; ++j) a1 = fmaf(__bfloat162float(W1[u * KP + j]), xs[j], a1);
+        h1[u] = a1 > 0.f ? a1 : 0.f;
+        __syncthreads();
+        float a2 = b2;
+        for (int k = 0; k < H; ++k) a2 = fmaf(__bfloat162float(W2[u * kH2 + k]), h1[k], a2);
+        float p = w3 * (a2 > 0.f ? a2 : 0.f);
+        for (int off = 16; off; off >>= 1) p += __shfl_xor_sync(full, p, off);
+        if ((u & 31) == 0) red[u >> 5] = p;
+        __syncthreads();
+        if (u == 0) {
+            const float out = red[0] + red[1] + b3;
+            const float s = scale[r];
+            beta_hat[r] = s > 0.f ? exp((double) out * sd + mu) / (double) s : -1.0;
+        }
+        __syncthreads();
+    }
+}
+
+size_t infer_smem(int K) {
+    const int KP = odd_stride(K);
+    return (((size_t) H * KP + (size_t) H * kH2) * 2 + 15) / 16 * 16 + sizeof(float) * (KP + H + 2);
+}
+
+// ---- warm-started calibration: safeguarded Newton on H(beta) = log(perplexity) --------------
+// H(beta) = beta <d> + log sum exp(-beta d) (the reference's formula, sum seeded with
+// DBL_MIN), decreasing in beta, dH/dbeta = -beta Var(d).  The bracket [lo, hi] shrinks with
+// every evaluation; a Newton step that leaves it, or a missing prediction, is replaced by
+// doubling / bisection as in the reference.
+__global__ void k_calibrate_warm(const double *__restrict__ dist, int stride, int offset, double *__restrict__ P,
+                                 int nrows, int K, double perplexity, const double *__restrict__ beta_hat,
+                                 int *__restrict__ iters, int *__restrict__ fallback) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    const double *d = dist + (size_t) r * stride + offset;
+    double *p = P + (size_t) r * K;
+    const double logU = log(perplexity);
+    const double tol = 1e-6;
+    double beta = beta_hat[r];
+    int fb = 0;
+    if (!(beta > 0.0) || !isfinite(beta)) {
+        beta = 1.0;
+        fb = 1;
+    }
+    double lo = 0.0, hi = HUGE_VAL, beta_eval = beta;
+    int it = 0;
+    while (it < 200) {
+        beta_eval = beta;
+        double sum_P = DBL_MIN, s1 = 0.0, s2 = 0.0;
+        for (int m = 0; m < K; ++m) {
+            const double e = exp(-beta * d[m]);
+            sum_P += e;
+            s1 += d[m] * e;
+            s2 += d[m] * d[m] * e;
+        }
+        const double Hv = beta * s1 / sum_P + log(sum_P);
+        ++it;
+        const double f = Hv - logU;
+        if (fabs(f) < tol) break;
+        if (f > 0.0)
+            lo = beta;
+        else
+            hi = beta;
+        const double ed = s1 / sum_P;
+        const double dH = -beta * (s2 / sum_P - ed * ed);
+        const double nb = dH < 0.0 ? beta - f / dH : -1.0;
+        if (nb > lo && nb < hi && isfinite(nb)) {
+            beta = nb;
+        } else {
+            fb = 1;
+            beta = isinf(hi) ? 2.0 * beta : 0.5 * (lo + hi);
+        }
+    }
+    double sum_P = DBL_MIN;
+    for (int m = 0; m < K; ++m) {
+        p[m] = exp(-beta_eval * d[m]);
+        sum_P += p[m];
+    }
+    for (int m = 0; m < K; ++m) p[m] /= sum_P;
+    iters[r] = it;
+    fallback[r] = fb;
+}
+
+uint64_t splitmix(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// He-uniform initial weights (fixed seed: training is reproducible up to FP32 atomics)
+std::vector<float> init_params(int K) {
+    const Offs o = offs(K);
+    std::vector<float> p((size_t) o.n, 0.f);
+    uint64_t s = 0x5EEDF17ull;
+    auto uni = [&s]() { return (float) ((splitmix(s) >> 11) * (1.0 / 9007199254740992.0)) * 2.f - 1.f; };
+    const float a1 = std::sqrt(6.f / (float) K), a2 = std::sqrt(6.f / (float) H);
+    for (int e = 0; e < H * K; ++e) p[o.w1 + e] = a1 * uni();
+    for (int e = 0; e < H * H; ++e) p[o.w2 + e] = a2 * uni();
+    for (int e = 0; e < H; ++e) p[o.w3 + e] = a2 * uni();
+    return p;
+}
+
+#define MCK(x)                                                         \
+    do {                                                               \
+        cudaError_t e_ = (x);                                          \
+        if (e_ != cudaSuccess) {                                       \
+            err = std::string(#x) + ": " + cudaGetErrorString(e_);     \
+            return -10;                                                \
+        }                                                              \
+    } while (0)
+
+// device buffers released on every path
+struct Bufs {
+    std::vector<void *> p;
+    template <typename T>
+    cudaError_t get(T **out, size_t n) {
+        void *v = nullptr;
+        cudaError_t e = cudaMalloc(&v, n * sizeof(T) + 16);
+        if (e == cudaSuccess) p.push_back(v);
+        *out = reinterpret_cast<T *>(v);
+        return e;
+    }
+    ~Bufs() {
+        for (void *v : p) cudaFree(v);
+    }
+};
+
+}  // namespace
+
+namespace {
+int g_calib_mode = -1;
+MlpStats g_calib_stats;
+std::mutex g_calib_mu;
+}  // namespace
+
+int calibration_mode() {
+    std::lock_guard<std::mutex> lk(g_calib_mu);
+    if (g_calib_mode < 0) {
+        const char *e = std::getenv("FITSNE_CALIBRATION");
+        g_calib_mode = (e && std::strcmp(e, "learned") == 0) ? 1 : 0;
+    }
+    return g_calib_mode;
+}
+void set_calibration_mode(int mode) {
+    std::lock_guard<std::mutex> lk(g_calib_mu);
+    g_calib_mode = mode == 1 ? 1 : 0;
+}
+void store_calibration_stats(const MlpStats &s) {
+    std::lock_guard<std::mutex> lk(g_calib_mu);
+    g_calib_stats = s;
+}
+MlpStats last_calibration_stats() {
+    std::lock_guard<std::mutex> lk(g_calib_mu);
+    return g_calib_stats;
+}
+
+int calibrate_rows_learned(const double *dist, int stride, int offset, double *P, int nrows, int K, double perplexity,
+                           cudaStream_t st, MlpStats *stats, std::string &err) {
+    MlpStats sx;
+    sx.rows = nrows;
+    const int nh = std::min(200000, std::max(10000, nrows / 10));
+    if (K > kMlpMaxIn || nrows < 2 * nh || perplexity <= 0) {
+        // too few rows to learn from: the plain bisection for all
+        std::vector<int> it;
+        const double t0 = now_ms();
+        int rc = calibrate_rows(dist, stride, offset, P, nrows, K, perplexity, 0.0, 0, nullptr, nullptr, st, err,
+                                &it);
+        if (rc) return rc;
+        sx.rows_harvest = nrows;
+        double s = 0;
+        for (int v : it) s += v;
+        sx.iters_plain = nrows ? s / nrows : 0;
+        sx.ms_harvest = now_ms() - t0;
+        if (stats) *stats = sx;
+        return 0;
+    }
+    sx.rows_harvest = nh;
+    Bufs b;
+    const Offs o = offs(K);
+    float *x = nullptr, *scale = nullptr, *target = nullptr, *params = nullptr, *grad = nullptr, *m = nullptr,
+          *v = nullptr, *hist = nullptr;
+    double *beta = nullptr, *loss = nullptr, *beta_hat = nullptr;
+    unsigned *step = nullptr;
+    int *iters = nullptr, *fb = nullptr;
+    MCK(b.get(&x, (size_t) nrows * K));
+    MCK(b.get(&scale, (size_t) nrows));
+    MCK(b.get(&target, (size_t) nh));
+    MCK(b.get(&beta, (size_t) nh));
+    MCK(b.get(&params, (size_t) o.n));
+    MCK(b.get(&grad, (size_t) o.n));
+    MCK(b.get(&m, (size_t) o.n));
+    MCK(b.get(&v, (size_t) o.n));
+    MCK(b.get(&loss, 1));
+    MCK(b.get(&step, 1));
+    MCK(b.get(&beta_hat, (size_t) (nrows - nh)));
+    MCK(b.get(&iters, (size_t) (nrows - nh)));
+    MCK(b.get(&fb, (size_t) (nrows - nh)));
+
+    // 1. harvest: the plain bisection (reference semantics) on the first nh rows
+    double t0 = now_ms();
+    std::vector<int> it_plain;
+    int rc = calibrate_rows(dist, stride, offset, P, nh, K, perplexity, 0.0, 0, nullptr, beta, st, err, &it_plain);
+    if (rc) return rc;
+    double s = 0;
+    for (int vv : it_plain) s += vv;
+    sx.iters_plain = s / nh;
+    sx.ms_harvest = now_ms() - t0;
+
+    // 2. features of every row, targets of the harvested ones; standardisation on the host
+    t0 = now_ms();
+    k_features<<<1024, 256, 0, st>>>(dist, stride, offset, nrows, K, nullptr, x, scale, nullptr);
+    k_features<<<1024, 256, 0, st>>>(dist, stride, offset, nh, K, beta, x, scale, target);
+    std::vector<float> ht(nh);
+    MCK(cudaMemcpyAsync(ht.data(), target, sizeof(float) * nh, cudaMemcpyDeviceToHost, st));
+    MCK(cudaStreamSynchronize(st));
+    double mu = 0, var = 0;
+    for (float t : ht) mu += t;
+    mu /= nh;
+    for (float t : ht) var += (t - mu) * (t - mu);
+    const double sd = std::max(1e-3, std::sqrt(var / nh));
+
+    // 3. training: Adam on random minibatches, kGraphSteps steps per captured graph
+    std::vector<float> p0 = init_params(K);
+    MCK(cudaMemcpyAsync(params, p0.data(), sizeof(float) * o.n, cudaMemcpyHostToDevice, st));
+    MCK(cudaMemsetAsync(grad, 0, sizeof(float) * o.n, st));
+    MCK(cudaMemsetAsync(m, 0, sizeof(float) * o.n, st));
+    MCK(cudaMemsetAsync(v, 0, sizeof(float) * o.n, st));
+    MCK(cudaMemsetAsync(loss, 0, sizeof(double), st));
+    MCK(cudaMemsetAsync(step, 0, sizeof(unsigned), st));
+    // about 8 passes over the harvest, at least 1000 and at most 3000 steps
+    const int nsteps = std::max(1000, std::min(3000, 8 * nh / kBatch)) / kGraphSteps * kGraphSteps;
+    MCK(b.get(&hist, (size_t) nsteps));
+    const size_t gsm = grad_smem(K);
+    MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) gsm));
+    const int gblocks = (kBatch + kSPB - 1) / kSPB;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    MCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < kGraphSteps; ++k) {
+        k_mlp_grad<<<gblocks, H, gsm, st>>>(params, K, x, target, nh, kBatch, (float) mu, (float) (1.0 / sd), step,
+                                            grad, loss);
+        k_adam<<<1, 1024, 0, st>>>(params, grad, m, v, o.n, step, loss, hist, kBatch);
+    }
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
+    for (int g = 0; ce == cudaSuccess && g < nsteps / kGraphSteps; ++g) ce = cudaGraphLaunch(exec, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+        err = std::string("mlp training: ") + cudaGetErrorString(ce);
+        return -10;
+    }
+    std::vector<float> hh(nsteps);
+    MCK(cudaMemcpy(hh.data(), hist, sizeof(float) * nsteps, cudaMemcpyDeviceToHost));
+    sx.train_steps = nsteps;
+    sx.loss_first = hh.front();
+    // the last ten steps' mean (minibatch noise)
+    double lt = 0;
+    for (int k = nsteps - 10; k < nsteps; ++k) lt += hh[k];
+    sx.loss_last = lt / 10;
+    sx.ms_train = now_ms() - t0;
+
+    // 4. inference for the remaining rows (BF16 weights)
+    t0 = now_ms();
+    const int nr = nrows - nh;
+    const size_t ism = infer_smem(K);
+    MCK(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) ism));
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    k_mlp_infer<<<nsm * 16, H, ism, st>>>(params, K, x + (size_t) nh * K, scale + nh, nr, (float) mu, (float) sd,
+                                          beta_hat);
+    MCK(cudaGetLastError());
+    MCK(cudaStreamSynchronize(st));
+    sx.ms_infer = now_ms() - t0;
+
+    // 5. warm-started calibration of the remaining rows
+    t0 = now_ms();
+    k_calibrate_warm<<<(nr + 127) / 128, 128, 0, st>>>(dist + (size_t) nh * stride, stride, offset, P + (size_t) nh * K,
+                                                        nr, K, perplexity, beta_hat, iters, fb);
+    MCK(cudaGetLastError());
+    std::vector<int> hi(nr), hf(nr);
+    MCK(cudaMemcpyAsync(hi.data(), iters, sizeof(int) * nr, cudaMemcpyDeviceToHost, st));
+    MCK(cudaMemcpyAsync(hf.data(), fb, sizeof(int) * nr, cudaMemcpyDeviceToHost, st));
+    MCK(cudaStreamSynchronize(st));
+    sx.ms_warm = now_ms() - t0;
+    double si = 0;
+    int nf = 0;
+    for (int k = 0; k < nr; ++k) {
+        si += hi[k];
+        nf += hf[k];
+    }
+    sx.iters_warm = si / nr;
+    sx.rows_fallback = nf;
+    if (stats) *stats = sx;
+    return 0;
+}
+
+int mlp_loss_grad_host(const float *params, int K, const double *dist, const double *beta, int nrows, double mu,
+                       double sd, float *grad, double *loss, std::string &err) {
+    if (K < 1 || K > kMlpMaxIn || nrows < 1) {
+        err = "invalid MLP shape";
+        return -3;
+    }
+    const Offs o = offs(K);
+    Bufs b;
+    float *dp = nullptr, *dg = nullptr, *x = nullptr, *scale = nullptr, *target = nullptr;
+    double *dd = nullptr, *db = nullptr, *dl = nullptr;
+    MCK(b.get(&dp, (size_t) o.n));
+    MCK(b.get(&dg, (size_t) o.n));
+    MCK(b.get(&dd, (size_t) nrows * K));
+    MCK(b.get(&db, (size_t) nrows));
+    MCK(b.get(&x, (size_t) nrows * K));
+    MCK(b.get(&scale, (size_t) nrows));
+    MCK(b.get(&target, (size_t) nrows));
+    MCK(b.get(&dl, 1));
+    MCK(cudaMemcpy(dp, params, sizeof(float) * o.n, cudaMemcpyHostToDevice));
+    MCK(cudaMemcpy(dd, dist, sizeof(double) * (size_t) nrows * K, cudaMemcpyHostToDevice));
+    MCK(cudaMemcpy(db, beta, sizeof(double) * nrows, cudaMemcpyHostToDevice));
+    MCK(cudaMemset(dg, 0, sizeof(float) * o.n));
+    MCK(cudaMemset(dl, 0, sizeof(double)));
+    k_features<<<256, 256>>>(dd, K, 0, nrows, K, db, x, scale, target);
+    const size_t gsm = grad_smem(K);
+    MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) gsm));
+    k_mlp_grad<<<(nrows + kSPB - 1) / kSPB, H, gsm>>>(dp, K, x, target, nrows, nrows, (float) mu, (float) (1.0 / sd),
+                                                      nullptr, dg, dl);
+    MCK(cudaGetLastError());
+    MCK(cudaDeviceSynchronize());
+    MCK(cudaMemcpy(grad, dg, sizeof(float) * o.n, cudaMemcpyDeviceToHost));
+    double l = 0;
+    MCK(cudaMemcpy(&l, dl, sizeof(double), cudaMemcpyDeviceToHost));
+    *loss = l / nrows;
+    return 0;
+}
+
+}  // namespace fitsne

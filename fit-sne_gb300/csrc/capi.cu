@@ -5,6 +5,7 @@
 #include <memory>
 #include <string>
 
+#include "calib_mlp.cuh"
 #include "../../include/fitsne_gb300.h"
 #include "capi_internal.h"
 #include "embedding.cuh"
@@ -216,6 +217,33 @@ void fitsne_session_destroy(fitsne_session *s) {
     s->impl.reset();
     if (st) cudaStreamDestroy(st);
     delete s;
+}
+
+void fitsne_set_calibration(int mode) { set_calibration_mode(mode); }
+int fitsne_get_calibration(void) { return calibration_mode(); }
+
+int fitsne_calibration_stats(double *out12) {
+    if (!out12) return set_error(FITSNE_E_ARG, "null argument");
+    const MlpStats s = last_calibration_stats();
+    const double v[12] = {(double) s.rows, (double) s.rows_harvest, (double) s.rows_fallback, (double) s.train_steps,
+                          s.iters_plain, s.iters_warm, s.loss_first, s.loss_last, s.ms_harvest, s.ms_train,
+                          s.ms_infer, s.ms_warm};
+    for (int k = 0; k < 12; ++k) out12[k] = v[k];
+    return 0;
+}
+
+int fitsne_mlp_param_count(int K) { return (K >= 1 && K <= kMlpMaxIn) ? (int) mlp_param_count(K) : -1; }
+
+int fitsne_mlp_loss_grad(const float *params, int K, const double *dist, const double *beta, int nrows, double mu,
+                         double sd, float *grad, double *loss) {
+    if (!params || !dist || !beta || !grad || !loss || nrows < 1 || K < 1 || K > kMlpMaxIn || !(sd > 0))
+        return set_error(FITSNE_E_ARG, "invalid arguments");
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    std::string err;
+    rc = mlp_loss_grad_host(params, K, dist, beta, nrows, mu, sd, grad, loss, err);
+    if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
+    return 0;
 }
 
 void fitsne_set_precision(int bits) { g_precision = (bits == 64) ? 64 : 32; }

@@ -1,9 +1,15 @@
 // Host driver of the per-iteration kernels (see embedding.cuh).
+#include <algorithm>
+#include <climits>
+#include <mutex>
+#include <map>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 
+#include "affinity.cuh"
 #include "embedding.cuh"
 #include "reorder.cuh"
 #include "sort.cuh"
@@ -11,49 +17,15 @@
 namespace fitsne {
 
 GridGeom make_grid_geom(double mn, double mx, int D, const GridParams &gp) {
-    GridGeom g;
-    std::memset(&g, 0, sizeof(g));
-    int nb = static_cast<int>(std::fmax((double) gp.min_num_intervals, (mx - mn) / gp.intervals_per_integer));
-    if (D == 2) {
-        // FFT-friendly box counts of computeFftGradient (tsne.cpp:1068-1077)
-        static const int allowed[20] = {25, 36, 50, 55, 60, 65, 70, 75, 80, 85,
-                                        90, 96, 100, 110, 120, 130, 140, 150, 175, 200};
-        if (nb < allowed[19]) {
-            int i = 0;
-            while (allowed[i] < nb) ++i;
-            nb = allowed[i];
-        }
-    }
-    if (nb < 1) nb = 1;
-    g.nb = nb;
-    g.nterms = gp.nterms;
-    g.M = nb * gp.nterms;
-    const double bw = (mx - mn) / (double) nb;
-    // n_body_fft_2d / nbodyfft read the lower corner and the width back from the box
-    // bounds array: lower[0] = 0*bw + mn, width = (1*bw + mn) - (0*bw + mn)
-    g.mn = 0.0 * bw + mn;
-    g.bw = (1.0 * bw + mn) - g.mn;
-    g.hk = bw / (double) gp.nterms;
-    const double h = 1.0 / (double) gp.nterms;
-    double s[kMaxInterp];
-    s[0] = h / 2.0;
-    for (int i = 1; i < gp.nterms && i < kMaxInterp; ++i) s[i] = s[i - 1] + h;
-    for (int i = 0; i < gp.nterms && i < kMaxInterp; ++i) {
-        double den = 1.0;
-        for (int j = 0; j < gp.nterms; ++j)
-            if (i != j) den *= s[i] - s[j];
-        g.s64[i] = s[i];
-        g.inv_den64[i] = 1.0 / den;
-        g.s32[i] = (float) s[i];
-        g.inv_den32[i] = (float) (1.0 / den);
-    }
-    return g;
+    return grid_geom(mn, mx, D, gp.nterms, gp.intervals_per_integer, gp.min_num_intervals, INT_MAX, nullptr);
 }
 
 template <typename T>
 Embedding<T>::Embedding() {
     const char *e = std::getenv("FITSNE_REORDER");
     if (e && std::atoi(e) == 0) reorder_enabled_ = false;
+    const char *g = std::getenv("FITSNE_GRAPH");
+    if (g && std::atoi(g) == 0) graphs_ = false;
 }
 
 template <typename T>
@@ -79,6 +51,13 @@ Embedding<T>::~Embedding() {
     cudaFree(red_mem_);
     cudaFree(red_cnt_);
     if (h_pin_) cudaFreeHost(h_pin_);
+    cudaFree(dgeom_);
+    cudaFree(gstatus_);
+    if (h_gstat_) cudaFreeHost(h_gstat_);
+    cudaFree(tw_dev_);
+    cudaFree(snap_);
+    cudaFree(snap_mean_);
+    if (gexec_) cudaGraphExecDestroy(gexec_);
     for (auto &b : evs_)
         for (auto &e : b)
             if (e) cudaEventDestroy(e);
@@ -227,6 +206,11 @@ int Embedding<T>::prepare_grid() {
         FITSNE_CK(cudaStreamSynchronize(st_));
         tw_[L] = d;
     }
+    return grid_buffers(M, L);
+}
+
+template <typename T>
+int Embedding<T>::grid_buffers(int M, int L) {
     const size_t H = L / 2 + 1;
     const size_t gridn = (D_ == 2) ? (size_t) M * M : (size_t) M;
     if (gridn > grid_cap_) {
@@ -291,8 +275,12 @@ int Embedding<T>::gradient(double *dC_host, double *sum_Q) {
     p.mode = 0;
     p.exag = 1.0;
     p.df = gp_.df;
+    if (attr_shape_ < 0) {
+        int tr = tune_attr();
+        if (tr) return tr;
+    }
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_, p,
-                                    red_, st_));
+                                    red_, st_, attr_shape_));
     launches_ += 2;
     std::vector<T> tmp((size_t) N_ * D_);
     FITSNE_CK(cudaMemcpyAsync(tmp.data(), dC_, sizeof(T) * tmp.size(), cudaMemcpyDeviceToHost, st_));
@@ -375,6 +363,7 @@ int Embedding<T>::reorder() {
     FITSNE_CK(cudaStreamSynchronize(st_));
     excl_ = (int) e0;
     reordered_ = true;
+    attr_shape_ = -1;
     return 0;
 }
 
@@ -393,8 +382,12 @@ int Embedding<T>::step(const UpdateParams &p, bool) {
     }
     rc = repulsion();
     if (rc) return rc;
+    if (attr_shape_ < 0) {
+        rc = tune_attr();
+        if (rc) return rc;
+    }
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], uY_, gains_, nullptr, rep_, N_, D_, p,
-                                    red_, st_));
+                                    red_, st_, attr_shape_));
     launches_ += 2;  // centre + attraction
     if (timing_) {
         FITSNE_CK(cudaEventRecord(evs_[tb_][5], st_));
@@ -458,6 +451,7 @@ int Embedding<T>::get_Y(double *Y_host) {
 
 template <typename T>
 int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *costs, bool verbose) {
+    if (graphs_ && !timing_ && it1 - it0 > 1) return run_schedule_graphs(s, it0, it1, costs, verbose);
     // replay the switches of tsne.cpp:533-544 for the iterations before it0
     double mult = s.early_exag_coeff;
     double momentum = s.momentum;
@@ -526,6 +520,338 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
         times_.attract = (float) (tacc_[4] / tacc_n_);
         times_.total = (float) (tacc_[5] / tacc_n_);
     }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Graph-captured iteration chunks.  The grid of every iteration is sized on the device
+// (k_geometry) inside a capacity chosen here; the host reads the status once per chunk.
+// Times the attraction pass (gradient only: no state changes) in each launch shape on this
+// embedding's data and keeps the fastest; choices are shared by embeddings of the same size
+// class (type, dimension, log2 N, log2 nnz / N, renumbered or not) within the process.
+template <typename T>
+int Embedding<T>::tune_attr() {
+    static std::mutex mu;
+    static std::map<std::vector<int>, int> chosen;
+    int lgN = 0, lgK = 0;
+    while ((1 << (lgN + 1)) <= N_) ++lgN;
+    const size_t per = N_ ? nnz_ / (size_t) N_ : 0;
+    while (((size_t) 1 << (lgK + 1)) <= per) ++lgK;
+    const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = chosen.find(key);
+        if (it != chosen.end()) {
+            attr_shape_ = it->second;
+            return 0;
+        }
+    }
+    const char *e = std::getenv("FITSNE_AUTOTUNE");
+    int best = 0;
+    if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
+        UpdateParams p{};
+        p.mode = 0;
+        p.exag = 1.0;
+        p.df = gp_.df;
+        cudaEvent_t a = nullptr, b = nullptr;
+        FITSNE_CK(cudaEventCreate(&a));
+        FITSNE_CK(cudaEventCreate(&b));
+        float best_ms = 0.f;
+        for (int sh = 0; sh < kNumAttrShapes; ++sh) {
+            FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_,
+                                            p, red_, st_, sh));
+            FITSNE_CK(cudaEventRecord(a, st_));
+            for (int r = 0; r < 3; ++r)
+                FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_,
+                                                D_, p, red_, st_, sh));
+            FITSNE_CK(cudaEventRecord(b, st_));
+            FITSNE_CK(cudaEventSynchronize(b));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            // another shape must beat the default by 3 % (timing noise)
+            if (sh == 0 || ms < 0.97f * best_ms) {
+                if (sh == 0 || ms < best_ms) {
+                    best = sh;
+                    best_ms = ms;
+                }
+            }
+        }
+        launches_ += 4 * kNumAttrShapes;
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (timing_requested()) {
+            int g = 0, u = 0;
+            attr_shape_info(best, &g, &u);
+            std::fprintf(stderr, "[fitsne] attraction launch shape (N=%d, nnz=%zu%s): %d rows per work item, %d edges "
+                                 "per lane\n", N_, nnz_, reordered_ ? ", renumbered" : "", g, u);
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        chosen[key] = best;
+    }
+    attr_shape_ = best;
+    return 0;
+}
+
+template <typename T>
+int Embedding<T>::plan_capacity(int grow) {
+    if (attr_shape_ < 0) {
+        int tr = tune_attr();
+        if (tr) return tr;
+    }
+    int nb = nb_last_ > 0 ? nb_last_ : geom_.nb;
+    if (nb < 1) nb = 1;
+    int target = grow ? std::max(nb_cap_ + 1, nb + nb / 2 + 1) : nb + nb / 4 + 1;
+    if (D_ == 2 && target < 200) {
+        static const int allowed[20] = {25, 36, 50, 55, 60, 65, 70, 75, 80, 85,
+                                        90, 96, 100, 110, 120, 130, 140, 150, 175, 200};
+        int i = 0;
+        while (allowed[i] < target) ++i;
+        target = allowed[i];
+    }
+    if (!grow && target <= nb_cap_) target = nb_cap_;  // keep a larger capacity (and the cached graph)
+    int M = target * gp_.nterms;
+    int L = smooth_even_at_least(2 * M);
+    while (L > max_fft_len<T>() && target > nb) {
+        --target;
+        M = target * gp_.nterms;
+        L = smooth_even_at_least(2 * M);
+    }
+    if (L > max_fft_len<T>()) {
+        err_ = "interpolation grid too large: " + std::to_string(L) + " > " + std::to_string(max_fft_len<T>());
+        return -13;
+    }
+    int rc = grid_buffers(M, L);
+    if (rc) return rc;
+    if (L > tw_dev_cap_) {
+        cudaFree(tw_dev_);
+        FITSNE_CK(cudaMalloc(&tw_dev_, sizeof(C) * L));
+        tw_dev_cap_ = L;
+    }
+    if (!dgeom_) {
+        const int W = y_width<T>(D_);
+        FITSNE_CK(cudaMalloc(&dgeom_, sizeof(DevGeom)));
+        FITSNE_CK(cudaMalloc(&gstatus_, sizeof(int)));
+        FITSNE_CK(cudaMallocHost(&h_gstat_, sizeof(int) * 2));
+        FITSNE_CK(cudaMalloc(&snap_, sizeof(T) * (size_t) N_ * (W + 2 * D_)));
+        FITSNE_CK(cudaMalloc(&snap_mean_, sizeof(double) * 2));
+    }
+    nb_cap_ = target;
+    M_cap_ = M;
+    L_cap_ = L;
+    return 0;
+}
+
+template <typename T>
+int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_first) {
+    const int W = y_width<T>(D_);
+    const size_t ny = (size_t) N_ * W, nd = (size_t) N_ * D_;
+    int c = cur_;
+    FITSNE_CK(cudaMemcpyAsync(snap_, Y_[c], sizeof(T) * ny, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemcpyAsync(snap_ + ny, uY_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemcpyAsync(snap_ + ny + nd, gains_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemcpyAsync(snap_mean_, red_.mean, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemsetAsync(gstatus_, 0, sizeof(int), st_));
+    const int mode = (gp_.df == 1.0) ? KERNEL_DF1 : KERNEL_VARDF;
+    const ConvGeom *cg =
+        reinterpret_cast<const ConvGeom *>(reinterpret_cast<const char *>(dgeom_) + offsetof(DevGeom, conv));
+    const size_t gridn = (D_ == 2) ? (size_t) M_cap_ * M_cap_ : (size_t) M_cap_;
+    for (int k = 0; k < len; ++k) {
+        FITSNE_CK(launch_center_minmax<T>(Y_[c], N_, D_, (k > 0 || apply_mean_first) ? 1 : 0, excl_, red_, st_));
+        FITSNE_CK(launch_geometry(red_, D_, gp_.nterms, gp_.intervals_per_integer, gp_.min_num_intervals, nb_cap_,
+                                  L_cap_, dgeom_, gstatus_, st_));
+        FITSNE_CK(twiddles_dev<T>(cg, tw_dev_, st_));
+        FITSNE_CK(cudaMemsetAsync(grid_in_, 0, sizeof(Cell4<T>) * gridn, st_));
+        FITSNE_CK(launch_spread_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_in_, st_));
+        if (D_ == 2)
+            FITSNE_CK(conv2d_launch_dev<T>(grid_in_, grid_out_, M_cap_, L_cap_, cg, tw_dev_, work_a_, work_b_, kspec_,
+                                           gp_.df, mode, st_));
+        else
+            FITSNE_CK(conv1d_launch_dev<T>(grid_in_, grid_out_, L_cap_, cg, tw_dev_, work_a_, gp_.df, mode, st_));
+        FITSNE_CK(launch_gather_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_out_, mode, rep_, red_, st_));
+        FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[c], Y_[1 - c], uY_, gains_, nullptr, rep_, N_, D_, p,
+                                        red_, st_, attr_shape_ < 0 ? 0 : attr_shape_));
+        c = 1 - c;
+    }
+    FITSNE_CK(cudaMemcpyAsync(h_gstat_, gstatus_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    FITSNE_CK(cudaMemcpyAsync(h_gstat_ + 1,
+                              reinterpret_cast<const char *>(dgeom_) + offsetof(DevGeom, g) + offsetof(GridGeom, nb),
+                              sizeof(int), cudaMemcpyDeviceToHost, st_));
+    gchunk_len_ = len;
+    gchunk_cur0_ = cur_;
+    return 0;
+}
+
+template <typename T>
+int Embedding<T>::finish_chunk(int len) {
+    const int status = h_gstat_[0];
+    if (status & 2) {
+        err_ = "embedding coordinates are not finite";
+        return -11;
+    }
+    if (status & 1) {
+        // the grid outgrew the capacity: back to the state at the start of the chunk
+        const int W = y_width<T>(D_);
+        const size_t ny = (size_t) N_ * W, nd = (size_t) N_ * D_;
+        FITSNE_CK(cudaMemcpyAsync(Y_[gchunk_cur0_], snap_, sizeof(T) * ny, cudaMemcpyDeviceToDevice, st_));
+        FITSNE_CK(cudaMemcpyAsync(uY_, snap_ + ny, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+        FITSNE_CK(cudaMemcpyAsync(gains_, snap_ + ny + nd, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+        FITSNE_CK(cudaMemcpyAsync(red_.mean, snap_mean_, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st_));
+        FITSNE_CK(cudaStreamSynchronize(st_));
+        cur_ = gchunk_cur0_;
+        return 1;
+    }
+    nb_last_ = h_gstat_[1];
+    if (len & 1) cur_ = 1 - cur_;
+    mean_pending_ = true;
+    launches_ += (unsigned long long) len * (D_ == 2 ? 11 : 8);
+    return 0;
+}
+
+template <typename T>
+std::vector<unsigned long long> Embedding<T>::chunk_key(const UpdateParams &p, int len) const {
+    std::vector<unsigned long long> key;
+    auto put = [&key](const void *v, size_t n) {
+        unsigned long long w = 0;
+        std::memcpy(&w, v, n < 8 ? n : 8);
+        key.push_back(w);
+    };
+    const bool am = mean_pending_;
+    put(&len, sizeof len);
+    put(&cur_, sizeof cur_);
+    put(&am, sizeof am);
+    put(&p.exag, 8);
+    put(&p.momentum, 8);
+    put(&p.learning_rate, 8);
+    put(&p.df, 8);
+    put(&p.max_step_norm, 8);
+    put(&p.use_gains, sizeof p.use_gains);
+    put(&nb_cap_, sizeof nb_cap_);
+    put(&excl_, sizeof excl_);
+    for (const void *q : {(const void *) row_, (const void *) col_, (const void *) val_, (const void *) Y_[0],
+                          (const void *) Y_[1], (const void *) uY_, (const void *) gains_, (const void *) rep_,
+                          (const void *) grid_in_, (const void *) grid_out_, (const void *) work_a_,
+                          (const void *) work_b_, (const void *) kspec_, (const void *) tw_dev_})
+        put(&q, sizeof q);
+    return key;
+}
+
+template <typename T>
+int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, double *costs, bool verbose) {
+    double mult = s.early_exag_coeff;
+    double momentum = s.momentum;
+    for (int it = 0; it < it0; ++it) {
+        if (it == s.stop_lying_iter) mult /= s.early_exag_coeff;
+        if (it == s.start_late_exag_iter) mult *= s.late_exag_coeff;
+        if (it == s.mom_switch_iter) momentum = s.final_momentum;
+    }
+    auto params = [&](int it) {
+        UpdateParams p{};
+        p.mode = 1;
+        p.exag = mult;
+        p.momentum = momentum;
+        p.learning_rate = s.learning_rate;
+        p.df = gp_.df;
+        if (s.no_momentum_during_exag) {
+            p.use_gains = (it > s.stop_lying_iter) ? 1 : 0;
+            p.max_step_norm = -1.0;
+        } else {
+            p.use_gains = 1;
+            p.max_step_norm = s.max_step_norm;
+        }
+        return p;
+    };
+    auto reorder_due = [&](int it) { return this->reorder_due(it, it0); };
+    auto kl_due = [&](int it) { return costs && ((it + 1) % 50 == 0 || it == s.max_iter - 1); };
+    auto after = [&](int it) -> int {  // the reference's switches and KL after iteration it
+        if (it == s.stop_lying_iter) mult /= s.early_exag_coeff;
+        if (it == s.start_late_exag_iter) mult *= s.late_exag_coeff;
+        if (it == s.mom_switch_iter) momentum = s.final_momentum;
+        if (kl_due(it)) {
+            double C = 0.0;
+            int rc = kl(mult, &C);
+            if (rc) return rc;
+            if (it < s.stop_lying_iter && s.stop_lying_iter != -1)
+                C = C / s.early_exag_coeff - std::log(s.early_exag_coeff);
+            if (it >= s.start_late_exag_iter && s.start_late_exag_iter != -1)
+                C = C / s.late_exag_coeff - std::log(s.late_exag_coeff);
+            costs[it] = C;
+            if (verbose) std::printf("Iteration %d, cost %f\n", it + 1, C);
+        }
+        return 0;
+    };
+    const unsigned long long l0 = launches_;
+    FITSNE_CK(cudaEventRecord(evr_[0], st_));
+    int it = it0;
+    if (it < it1) {
+        // first iteration on the host path: it sizes the grid and fixes the launch shapes
+        if (reorder_due(it)) {
+            int rr = reorder();
+            if (rr) return rr;
+        }
+        int rc = step(params(it), it == 0);
+        if (rc) return rc;
+        nb_last_ = geom_.nb;
+        rc = after(it);
+        if (rc) return rc;
+        ++it;
+    }
+    while (it < it1) {
+        if (reorder_due(it)) {
+            int rr = reorder();
+            if (rr) return rr;
+        }
+        int end = it + 1;
+        while (end < it1 && !(kl_due(end - 1) || end - 1 == s.stop_lying_iter || end - 1 == s.start_late_exag_iter ||
+                              end - 1 == s.mom_switch_iter || reorder_due(end)))
+            ++end;
+        const int len = end - it;
+        const UpdateParams p = params(it);
+        int grow = 0;
+        while (true) {
+            int rc = plan_capacity(grow);
+            if (rc) return rc;
+            const bool am = mean_pending_;
+            const std::vector<unsigned long long> key = chunk_key(p, len);
+            if (!gexec_ || key != gkey_) {
+                if (gexec_) {
+                    cudaGraphExecDestroy(gexec_);
+                    gexec_ = nullptr;
+                }
+                cudaGraph_t graph = nullptr;
+                FITSNE_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeRelaxed));
+                rc = record_chunk(p, len, am);
+                cudaError_t ce = cudaStreamEndCapture(st_, &graph);
+                if (rc) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return rc;
+                }
+                if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec_, graph, 0);
+                if (graph) cudaGraphDestroy(graph);
+                if (ce != cudaSuccess) return fail("chunk graph", ce);
+                gkey_ = key;
+                gchunk_cur0_ = cur_;
+                gchunk_len_ = len;
+            }
+            gchunk_cur0_ = cur_;
+            FITSNE_CK(cudaGraphLaunch(gexec_, st_));
+            FITSNE_CK(cudaStreamSynchronize(st_));
+            rc = finish_chunk(len);
+            if (rc < 0) return rc;
+            if (rc == 0) break;
+            grow = 1;  // the embedding outgrew the capacity inside the chunk: larger grid, same chunk
+        }
+        for (int k = it; k < end; ++k) {
+            int rc = after(k);
+            if (rc) return rc;
+        }
+        it = end;
+    }
+    FITSNE_CK(cudaEventRecord(evr_[1], st_));
+    FITSNE_CK(cudaEventSynchronize(evr_[1]));
+    cudaEventElapsedTime(&times_.run_ms, evr_[0], evr_[1]);
+    times_.launches = launches_ - l0;
     return 0;
 }
 

@@ -79,6 +79,34 @@ class Embedding {
     int run_schedule(const Schedule &s, int it0, int it1, double *costs, bool verbose);
 
     void set_timing(bool on) { timing_ = on; }
+    // CUDA-graph iteration chunks (on by default; FITSNE_GRAPH=0 or timing turn them off)
+    void set_graphs(bool on) { graphs_ = on; }
+    bool graphs() const { return graphs_; }
+
+    // ---- graph-captured chunks (used by run_schedule and by the batched driver) ----
+    // A chunk is `len` iterations with constant parameters, recorded on this object's
+    // stream (which must be capturing, or is captured by the caller): snapshot of the state,
+    // then per iteration centre/min-max, device-side grid sizing, spread, convolution,
+    // gather, attraction + update; status and box count copied to pinned memory at the end.
+    int record_chunk(const UpdateParams &p, int len, bool apply_mean_first);
+    // After the chunk ran: 0 ok, 1 the grid outgrew its capacity (state restored: redo the
+    // chunk with a larger one), <0 error.  Updates cur_ / mean_pending_ on success.
+    int finish_chunk(int len);
+    // Capacity for the next chunk from the last known box count (grows buffers; call
+    // outside any capture).  grow > 0 forces a larger capacity after an overflow.
+    int plan_capacity(int grow);
+    // Runs iterations [it0, it1) with graph chunks; costs may be null.
+    int run_schedule_graphs(const Schedule &s, int it0, int it1, double *costs, bool verbose);
+    // What a recorded chunk depends on (parameters, capacity, buffers): equal keys replay.
+    std::vector<unsigned long long> chunk_key(const UpdateParams &p, int len) const;
+    bool mean_pending() const { return mean_pending_; }
+    void set_first_geometry() { nb_last_ = geom_.nb; }
+    // Renumbering rule of run_schedule (iterations 50, 150, 300, 600 above kReorderMinN).
+    bool reorder_due(int it, int it0) const {
+        return reorder_enabled_ && N_ >= kReorderMinN &&
+               (it == 50 || it == 150 || it == 300 || it == 600 || (!reordered_ && it == it0 && it0 > 50));
+    }
+    int reorder_now() { return reorder(); }
     const StageTimes &last_times() const { return times_; }
     const GridGeom &last_geom() const { return geom_; }
     int last_L() const { return L_; }
@@ -134,6 +162,26 @@ class Embedding {
     int tacc_n_ = 0;
     void read_stage_events(int buf);
     unsigned long long launches_ = 0;  // running count of this object's kernel launches
+
+    // autotuned launch shape of the attraction pass (-1: not chosen yet); re-chosen after a
+    // locality renumbering, since the gathers' locality decides between the shapes
+    int attr_shape_ = -1;
+    int tune_attr();
+    // graph chunks
+    bool graphs_ = true;
+    DevGeom *dgeom_ = nullptr;         // device: geometry of the current iteration
+    int *gstatus_ = nullptr;           // device: OR of the chunk's geometry statuses
+    int *h_gstat_ = nullptr;           // pinned: [status, boxes per dimension]
+    C *tw_dev_ = nullptr;              // twiddles written on the device for the current L
+    int tw_dev_cap_ = 0;
+    int nb_cap_ = 0, M_cap_ = 0, L_cap_ = 0, nb_last_ = 0;
+    T *snap_ = nullptr;                // state at the start of a chunk: Y, uY, gains
+    double *snap_mean_ = nullptr;      // and the pending mean
+    cudaGraphExec_t gexec_ = nullptr;  // cached chunk graph and its key
+    std::vector<unsigned long long> gkey_;
+    int grid_buffers(int M, int L);    // grows grid / FFT buffers to M x M, L
+    int gchunk_len_ = 0;
+    int gchunk_cur0_ = 0;
 
     // locality renumbering (reorder.cuh): perm_[k] = caller index of internal point k
     int reorder();

@@ -16,28 +16,6 @@
 
 namespace fitsne {
 
-bool make_fft_plan(int L, FftPlan *p) {
-    p->L = L;
-    p->nst = 0;
-    int n = L;
-    while (n % 4 == 0 && p->nst < 24) { p->radix[p->nst++] = 4; n /= 4; }
-    while (n % 2 == 0 && p->nst < 24) { p->radix[p->nst++] = 2; n /= 2; }
-    while (n % 3 == 0 && p->nst < 24) { p->radix[p->nst++] = 3; n /= 3; }
-    while (n % 5 == 0 && p->nst < 24) { p->radix[p->nst++] = 5; n /= 5; }
-    return n == 1 && L >= 2;
-}
-
-int smooth_even_at_least(int n) {
-    for (int m = n < 2 ? 2 : n;; ++m) {
-        if (m & 1) continue;
-        int k = m;
-        while (k % 2 == 0) k /= 2;
-        while (k % 3 == 0) k /= 3;
-        while (k % 5 == 0) k /= 5;
-        if (k == 1) return m;
-    }
-}
-
 namespace {
 
 template <typename C>
@@ -227,8 +205,15 @@ FITSNE_D void unpack_r2c(const C *Zs, int L, int kb, C &F, C &G) {
 
 template <typename T>
 __global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
-                              typename Cx<T>::t *__restrict__ krow, T h, T df, int mode) {
+                              typename Cx<T>::t *__restrict__ krow, T h, T df, int mode,
+                              const ConvGeom *__restrict__ cg) {
     typedef typename Cx<T>::t C;
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+        h = (T) cg->h;
+        if ((int) blockIdx.x >= 2 * M - 1) return;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *bufa = reinterpret_cast<C *>(smem_raw);
@@ -260,8 +245,14 @@ __global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__rest
 
 template <typename T>
 __global__ void k_kernel_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
-                              const typename Cx<T>::t *__restrict__ krow, KSpec<T> *__restrict__ kspec) {
+                              const typename Cx<T>::t *__restrict__ krow, KSpec<T> *__restrict__ kspec,
+                              const ConvGeom *__restrict__ cg) {
     typedef typename Cx<T>::t C;
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+        if ((int) blockIdx.x >= pl.L / 2 + 1) return;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *spec = reinterpret_cast<C *>(smem_raw);
@@ -293,8 +284,14 @@ __global__ void k_kernel_cols(int M, FftPlan pl, const typename Cx<T>::t *__rest
 
 template <typename T>
 __global__ void k_data_rows(const Cell4<T> *__restrict__ grid, int M, FftPlan pl,
-                            const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ d1) {
+                            const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ d1,
+                            const ConvGeom *__restrict__ cg) {
     typedef typename Cx<T>::t C;
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+        if ((int) blockIdx.x >= M) return;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *bufa = reinterpret_cast<C *>(smem_raw);
@@ -325,8 +322,13 @@ __global__ void k_data_rows(const Cell4<T> *__restrict__ grid, int M, FftPlan pl
 template <typename T>
 __global__ void k_data_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
                             const typename Cx<T>::t *__restrict__ d1, const KSpec<T> *__restrict__ kspec,
-                            typename Cx<T>::t *__restrict__ d2, int mode) {
+                            typename Cx<T>::t *__restrict__ d2, int mode, const ConvGeom *__restrict__ cg) {
     typedef typename Cx<T>::t C;
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+        if ((int) blockIdx.x >= pl.L / 2 + 1) return;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *spec = reinterpret_cast<C *>(smem_raw);
@@ -376,8 +378,14 @@ __global__ void k_data_cols(int M, FftPlan pl, const typename Cx<T>::t *__restri
 
 template <typename T>
 __global__ void k_data_rows_inv(const typename Cx<T>::t *__restrict__ d2, int M, FftPlan pl,
-                                const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out) {
+                                const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out,
+                                const ConvGeom *__restrict__ cg) {
     typedef typename Cx<T>::t C;
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+        if ((int) blockIdx.x >= M) return;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *bufa = reinterpret_cast<C *>(smem_raw);
@@ -419,8 +427,13 @@ __global__ void k_data_rows_inv(const typename Cx<T>::t *__restrict__ d2, int M,
 template <typename T>
 __global__ void k_conv1d_fwd(const Cell4<T> *__restrict__ grid, int M, FftPlan pl,
                              const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ work, T h,
-                             T df, int mode) {
+                             T df, int mode, const ConvGeom *__restrict__ cg) {
     typedef typename Cx<T>::t C;
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+        h = (T) cg->h;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L;
     C *bufa = reinterpret_cast<C *>(smem_raw);
@@ -447,8 +460,13 @@ __global__ void k_conv1d_fwd(const Cell4<T> *__restrict__ grid, int M, FftPlan p
 
 template <typename T>
 __global__ void k_conv1d_inv(const typename Cx<T>::t *__restrict__ work, int M, FftPlan pl,
-                             const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out, int mode) {
+                             const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out, int mode,
+                             const ConvGeom *__restrict__ cg) {
     typedef typename Cx<T>::t C;
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L;
     C *bufa = reinterpret_cast<C *>(smem_raw);
@@ -504,11 +522,36 @@ cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
     if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
     const int thr = 256;
     // kernel spectra: krow uses work_a ([4][L][H]); data passes use work_b ([4][M][H]) then work_a
-    k_kernel_rows<T><<<2 * M - 1, thr, s4, st>>>(M, plan, tw, work_a, (T) h, (T) df, mode);
-    k_kernel_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_a, kspec);
-    k_data_rows<T><<<M, thr, s4, st>>>(grid_in, M, plan, tw, work_b);
-    k_data_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_b, kspec, work_a, mode);
-    k_data_rows_inv<T><<<M, thr, s4, st>>>(work_a, M, plan, tw, grid_out);
+    k_kernel_rows<T><<<2 * M - 1, thr, s4, st>>>(M, plan, tw, work_a, (T) h, (T) df, mode, nullptr);
+    k_kernel_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_a, kspec, nullptr);
+    k_data_rows<T><<<M, thr, s4, st>>>(grid_in, M, plan, tw, work_b, nullptr);
+    k_data_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_b, kspec, work_a, mode, nullptr);
+    k_data_rows_inv<T><<<M, thr, s4, st>>>(work_a, M, plan, tw, grid_out, nullptr);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t conv2d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M_cap, int L_cap, const ConvGeom *cg,
+                              const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
+                              KSpec<T> *kspec, double df, int mode, cudaStream_t st) {
+    typedef typename Cx<T>::t C;
+    const int H = L_cap / 2 + 1;
+    if (L_cap > max_fft_len<T>() || L_cap < 2 * M_cap) return cudaErrorInvalidValue;
+    const size_t s4 = 4 * (size_t) L_cap * sizeof(C);
+    const size_t s5 = 5 * (size_t) L_cap * sizeof(C);
+    cudaError_t e;
+    if ((e = set_smem(k_kernel_rows<T>, s4)) != cudaSuccess) return e;
+    if ((e = set_smem(k_kernel_cols<T>, s5)) != cudaSuccess) return e;
+    if ((e = set_smem(k_data_rows<T>, s4)) != cudaSuccess) return e;
+    if ((e = set_smem(k_data_cols<T>, s5)) != cudaSuccess) return e;
+    if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
+    const int thr = 256;
+    FftPlan dummy{};
+    k_kernel_rows<T><<<2 * M_cap - 1, thr, s4, st>>>(0, dummy, tw, work_a, T(0), (T) df, mode, cg);
+    k_kernel_cols<T><<<H, thr, s5, st>>>(0, dummy, tw, work_a, kspec, cg);
+    k_data_rows<T><<<M_cap, thr, s4, st>>>(grid_in, 0, dummy, tw, work_b, cg);
+    k_data_cols<T><<<H, thr, s5, st>>>(0, dummy, tw, work_b, kspec, work_a, mode, cg);
+    k_data_rows_inv<T><<<M_cap, thr, s4, st>>>(work_a, 0, dummy, tw, grid_out, cg);
     return cudaGetLastError();
 }
 
@@ -523,8 +566,42 @@ cudaError_t conv1d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
     cudaError_t e;
     if ((e = set_smem(k_conv1d_fwd<T>, s2)) != cudaSuccess) return e;
     if ((e = set_smem(k_conv1d_inv<T>, s2)) != cudaSuccess) return e;
-    k_conv1d_fwd<T><<<6, 512, s2, st>>>(grid_in, M, plan, tw, work, (T) h, (T) df, mode);
-    k_conv1d_inv<T><<<3, 512, s2, st>>>(work, M, plan, tw, grid_out, mode);
+    k_conv1d_fwd<T><<<6, 512, s2, st>>>(grid_in, M, plan, tw, work, (T) h, (T) df, mode, nullptr);
+    k_conv1d_inv<T><<<3, 512, s2, st>>>(work, M, plan, tw, grid_out, mode, nullptr);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t conv1d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int L_cap, const ConvGeom *cg,
+                              const typename Cx<T>::t *tw, typename Cx<T>::t *work, double df, int mode,
+                              cudaStream_t st) {
+    typedef typename Cx<T>::t C;
+    const size_t s2 = 2 * (size_t) L_cap * sizeof(C);
+    if (s2 > 227 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if ((e = set_smem(k_conv1d_fwd<T>, s2)) != cudaSuccess) return e;
+    if ((e = set_smem(k_conv1d_inv<T>, s2)) != cudaSuccess) return e;
+    FftPlan dummy{};
+    k_conv1d_fwd<T><<<6, 512, s2, st>>>(grid_in, 0, dummy, tw, work, T(0), (T) df, mode, cg);
+    k_conv1d_inv<T><<<3, 512, s2, st>>>(work, 0, dummy, tw, grid_out, mode, cg);
+    return cudaGetLastError();
+}
+
+namespace {
+template <typename T>
+__global__ void k_twiddles_geom(const ConvGeom *__restrict__ cg, typename Cx<T>::t *__restrict__ tw) {
+    const int L = cg->plan.L;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < L; j += gridDim.x * blockDim.x) {
+        double sn, cs;
+        sincospi(2.0 * (double) j / (double) L, &sn, &cs);
+        tw[j] = mkc((T) cs, (T) -sn);
+    }
+}
+}  // namespace
+
+template <typename T>
+cudaError_t twiddles_dev(const ConvGeom *cg, typename Cx<T>::t *tw, cudaStream_t st) {
+    k_twiddles_geom<T><<<8, 256, 0, st>>>(cg, tw);
     return cudaGetLastError();
 }
 
@@ -537,5 +614,17 @@ template cudaError_t conv1d_launch<float>(const Cell4<float> *, Cell4<float> *, 
                                           float2 *, double, double, int, cudaStream_t);
 template cudaError_t conv1d_launch<double>(const Cell4<double> *, Cell4<double> *, int, const FftPlan &,
                                            const double2 *, double2 *, double, double, int, cudaStream_t);
+template cudaError_t conv2d_launch_dev<float>(const Cell4<float> *, Cell4<float> *, int, int, const ConvGeom *,
+                                              const float2 *, float2 *, float2 *, KSpec<float> *, double, int,
+                                              cudaStream_t);
+template cudaError_t conv2d_launch_dev<double>(const Cell4<double> *, Cell4<double> *, int, int, const ConvGeom *,
+                                               const double2 *, double2 *, double2 *, KSpec<double> *, double, int,
+                                               cudaStream_t);
+template cudaError_t conv1d_launch_dev<float>(const Cell4<float> *, Cell4<float> *, int, const ConvGeom *,
+                                              const float2 *, float2 *, double, int, cudaStream_t);
+template cudaError_t conv1d_launch_dev<double>(const Cell4<double> *, Cell4<double> *, int, const ConvGeom *,
+                                               const double2 *, double2 *, double, int, cudaStream_t);
+template cudaError_t twiddles_dev<float>(const ConvGeom *, float2 *, cudaStream_t);
+template cudaError_t twiddles_dev<double>(const ConvGeom *, double2 *, cudaStream_t);
 
 }  // namespace fitsne

@@ -27,9 +27,38 @@ struct FftPlan {
 };
 
 // Builds the pass list for a 5-smooth L; returns false if L has another prime factor.
-bool make_fft_plan(int L, FftPlan *plan);
+FITSNE_HD bool make_fft_plan(int L, FftPlan *p) {
+    p->L = L;
+    p->nst = 0;
+    int n = L;
+    while (n % 4 == 0 && p->nst < 24) { p->radix[p->nst++] = 4; n /= 4; }
+    while (n % 2 == 0 && p->nst < 24) { p->radix[p->nst++] = 2; n /= 2; }
+    while (n % 3 == 0 && p->nst < 24) { p->radix[p->nst++] = 3; n /= 3; }
+    while (n % 5 == 0 && p->nst < 24) { p->radix[p->nst++] = 5; n /= 5; }
+    return n == 1 && L >= 2;
+}
+
 // Smallest even 5-smooth integer >= n.
-int smooth_even_at_least(int n);
+FITSNE_HD int smooth_even_at_least(int n) {
+    for (int m = n < 2 ? 2 : n;; ++m) {
+        if (m & 1) continue;
+        int k = m;
+        while (k % 2 == 0) k /= 2;
+        while (k % 3 == 0) k /= 3;
+        while (k % 5 == 0) k /= 5;
+        if (k == 1) return m;
+    }
+}
+
+// Convolution geometry kept in device memory, written each iteration by the kernel that
+// sizes the interpolation grid, so that an iteration needs no host decision (and can be
+// captured in a CUDA graph).  Kernels launched for a capacity (M_cap, L_cap) read it and
+// idle the blocks beyond the current M and L.
+struct ConvGeom {
+    int M;         // nodes per dimension
+    double h;      // node spacing of the kernel samples
+    FftPlan plan;  // passes of the current L (plan.L)
+};
 
 // Largest transform length the shared-memory passes accept for each precision.
 constexpr int kMaxL32 = 5760;
@@ -58,6 +87,21 @@ template <typename T>
 cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, const FftPlan &plan,
                           const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
                           KSpec<T> *kspec, double h, double df, int mode, cudaStream_t st);
+
+// As conv2d_launch with the geometry read from device memory (cg); grids and shared
+// memory sized for M_cap and L_cap (cg->M <= M_cap, cg->plan.L <= L_cap; tw holds the
+// twiddles of cg->plan.L).
+template <typename T>
+cudaError_t conv2d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M_cap, int L_cap, const ConvGeom *cg,
+                              const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
+                              KSpec<T> *kspec, double df, int mode, cudaStream_t st);
+template <typename T>
+cudaError_t conv1d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int L_cap, const ConvGeom *cg,
+                              const typename Cx<T>::t *tw, typename Cx<T>::t *work, double df, int mode,
+                              cudaStream_t st);
+// tw[j] = exp(-2 pi i j / L) for the L of cg (FP64 sincospi, rounded to T).
+template <typename T>
+cudaError_t twiddles_dev(const ConvGeom *cg, typename Cx<T>::t *tw, cudaStream_t st);
 
 // 1-D: grid_in/out hold 4 fields per node (only the first 3 are used); work holds 6*L
 // complex values.

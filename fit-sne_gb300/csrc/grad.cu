@@ -1,4 +1,5 @@
 // Per-point and per-edge kernels of one FIt-SNE gradient iteration (see grad.cuh).
+#include <algorithm>
 #include <cfloat>
 
 #include "grad.cuh"
@@ -8,8 +9,11 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kRedGrid = 1216;  // 152 SMs x 8 resident blocks of 256 threads
-constexpr int kAttrUnroll = 4;  // CSR edges per lane per batch in the attraction pass
-constexpr int kAttrGroup = 16;  // consecutive rows per work item of the attraction pass (<= 32)
+// Launch shapes of the attraction pass: consecutive rows per work item (<= 32) and CSR
+// edges per lane per batch.  Entry 0 is the default; Embedding's autotuner times the rest.
+// Shape 5: the 8 warps of a block take 8 consecutive groups at once, so that the neighbour
+// gathers of an SM's warps overlap in its L1.
+constexpr int kAttrShapes[kNumAttrShapes][2] = {{16, 4}, {32, 4}, {8, 4}, {16, 2}, {32, 2}, {16, 4}};
 
 // ---------------------------------------------------------------------------------
 // storage layouts of Y
@@ -85,7 +89,7 @@ struct BoxP<double> {
     double s[kMaxInterp], inv_den[kMaxInterp];
 };
 
-BoxP<float> make_box(const GridGeom &g, float *) {
+__host__ __device__ BoxP<float> make_box(const GridGeom &g, float *) {
     BoxP<float> b;
     b.neg_mn = df_from_double(-g.mn);
     b.bw = df_from_double(g.bw);
@@ -102,7 +106,7 @@ BoxP<float> make_box(const GridGeom &g, float *) {
     }
     return b;
 }
-BoxP<double> make_box(const GridGeom &g, double *) {
+__host__ __device__ BoxP<double> make_box(const GridGeom &g, double *) {
     BoxP<double> b;
     b.mn = g.mn;
     b.bw = g.bw;
@@ -327,8 +331,9 @@ __global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply
 // spread (step 1 of n_body_fft_2d / nbodyfft) in box-local charges
 template <typename T, int D, int NT>
 __global__ void __launch_bounds__(kBlock) k_spread(const T *__restrict__ Y, int N, BoxP<T> b,
-                                                   Cell4<T> *__restrict__ grid) {
+                                                   Cell4<T> *__restrict__ grid, const DevGeom *__restrict__ dg) {
     typedef typename YL<T, D>::P P;
+    if (dg) b = make_box(dg->g, (T *) nullptr);
     const int n = NT > 0 ? NT : b.nterms;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         P c[D];
@@ -369,13 +374,123 @@ __global__ void __launch_bounds__(kBlock) k_spread(const T *__restrict__ Y, int 
     }
 }
 
+// FP32 spread with nterms = 3, aggregated per warp before the atomics.  After the locality
+// renumbering consecutive points mostly share a box, and every point of a box charges the
+// same 9 (2-D) or 3 (1-D) nodes: a segmented inclusive scan over runs of equal box index
+// (head flags where the box changes, five shuffle steps per charge value) leaves each run's
+// sums in its last lane, which alone issues the node atomics.  Identical charges to
+// k_spread; only the order of the FP32 additions differs.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_spread_runs(const float *__restrict__ Y, int N, BoxP<float> b,
+                                                        Cell4<float> *__restrict__ grid,
+                                                        const DevGeom *__restrict__ dg) {
+    constexpr int NT = 3;
+    if (dg) b = make_box(dg->g, (float *) nullptr);
+    constexpr int NV = (D == 2) ? NT * NT : NT;  // nodes per point
+    constexpr int NC = (D == 2) ? 4 : 3;         // charge values per node
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = warp0 * 32; base < N; base += nwarps * 32) {
+        const int i = base + lane;
+        const bool valid = i < N;
+        int bx[D];
+        float t[D];
+        float w[D][NT];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            bx[d] = 0;
+            t[d] = 0.5f;
+#pragma unroll
+            for (int k = 0; k < NT; ++k) w[d][k] = 0.f;
+        }
+        if (valid) {
+            df32 c[D];
+            YL<float, D>::load(Y, i, c);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                box_coord(c[d], b, bx[d], t[d]);
+                lagrange<float, NT>(t[d], b, w[d]);
+            }
+        }
+        const int key = valid ? (D == 2 ? bx[0] * b.nb + bx[1] : bx[0]) : -1 - lane;
+        float v[NV][NC];
+        if constexpr (D == 2) {
+#pragma unroll
+            for (int ia = 0; ia < NT; ++ia) {
+                const float ux = (t[0] - b.s[ia]) * b.bwT;
+#pragma unroll
+                for (int ib = 0; ib < NT; ++ib) {
+                    const float uy = (t[1] - b.s[ib]) * b.bwT;
+                    const float ww = w[0][ia] * w[1][ib];
+                    float *o = v[ia * NT + ib];
+                    o[0] = ww;
+                    o[1] = ww * ux;
+                    o[2] = ww * uy;
+                    o[3] = ww * (ux * ux + uy * uy);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int ia = 0; ia < NT; ++ia) {
+                const float u = (t[0] - b.s[ia]) * b.bwT;
+                const float ww = w[0][ia];
+                v[ia][0] = ww;
+                v[ia][1] = ww * u;
+                v[ia][2] = ww * u * u;
+            }
+        }
+        // segmented inclusive scan: after the step with offset `off`, lane l holds the sum
+        // over [max(head(l), l - 2 off + 1), l]
+        const int prev = __shfl_up_sync(full, key, 1);
+        const unsigned heads = __ballot_sync(full, lane == 0 || prev != key);
+        const int my_head = 31 - __clz(heads & (full >> (31 - lane)));
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const bool take = lane - off >= my_head;
+#pragma unroll
+            for (int q = 0; q < NV; ++q)
+#pragma unroll
+                for (int r = 0; r < NC; ++r) {
+                    const float y = __shfl_up_sync(full, v[q][r], off);
+                    if (take) v[q][r] += y;
+                }
+        }
+        const int next = __shfl_down_sync(full, key, 1);
+        if (valid && (lane == 31 || next != key)) {
+            if constexpr (D == 2) {
+#pragma unroll
+                for (int ia = 0; ia < NT; ++ia) {
+                    const size_t rowbase = (size_t) (bx[0] * NT + ia) * b.M + bx[1] * NT;
+#pragma unroll
+                    for (int ib = 0; ib < NT; ++ib) {
+                        const float *o = v[ia * NT + ib];
+                        atomicAdd(reinterpret_cast<float4 *>(grid + rowbase + ib), make_float4(o[0], o[1], o[2], o[3]));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int ia = 0; ia < NT; ++ia) {
+                    float *cell = reinterpret_cast<float *>(grid + bx[0] * NT + ia);
+                    atomicAdd(cell + 0, v[ia][0]);
+                    atomicAdd(cell + 1, v[ia][1]);
+                    atomicAdd(cell + 2, v[ia][2]);
+                }
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------
 // gather (step 3) + the repulsion numerators + Z
 template <typename T, int D, int NT>
 __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int N, BoxP<T> b,
                                                    const Cell4<T> *__restrict__ pot, int mode,
-                                                   T *__restrict__ rep, RedScratch r) {
+                                                   T *__restrict__ rep, RedScratch r,
+                                                   const DevGeom *__restrict__ dg) {
     typedef typename YL<T, D>::P P;
+    if (dg) b = make_box(dg->g, (T *) nullptr);
     __shared__ double sh[32];
     const int n = NT > 0 ? NT : b.nterms;
     double zacc[1] = {0.0};
@@ -439,7 +554,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 // remain: the CSR entries (prefetched into L2 while the previous row is processed) and the
 // neighbour Y gathers (L2-resident).  Within a row, lanes take kAttrUnroll edges each per
 // batch: all index / value loads first, then all gathers.
-template <typename T, int D>
+template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups = false>
 __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
                                                  const T *__restrict__ val, const T *__restrict__ Yin,
                                                  T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
@@ -464,11 +579,22 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
         else
             msum[d] = 0.0;
     }
+    __shared__ int block_item;
     while (true) {
         int g = 0;
-        if (lane == 0) g = (int) atomicAdd(r.count + 4, 1u);
-        g = __shfl_sync(full, g, 0);
-        if (g >= ngroups) break;
+        if constexpr (kBlockGroups) {
+            __syncthreads();  // every warp has read the previous item
+            if (threadIdx.x == 0) block_item = (int) atomicAdd(r.count + 4, 1u);
+            __syncthreads();
+            const int wpb = blockDim.x >> 5;
+            if (block_item * wpb >= ngroups) break;  // uniform over the block
+            g = block_item * wpb + (threadIdx.x >> 5);
+            if (g >= ngroups) continue;
+        } else {
+            if (lane == 0) g = (int) atomicAdd(r.count + 4, 1u);
+            g = __shfl_sync(full, g, 0);
+            if (g >= ngroups) break;
+        }
         const int i0 = g * kAttrGroup;
         const int nr = min(kAttrGroup, N - i0);
         const int my = i0 + lane;
@@ -707,19 +833,59 @@ cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, int excl, R
 }
 
 template <typename T>
-cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &gg, Cell4<T> *grid, cudaStream_t st) {
-    const BoxP<T> b = make_box(gg, (T *) nullptr);
+cudaError_t spread_impl(const T *Y, int N, int D, int nterms, const BoxP<T> &b, Cell4<T> *grid, const DevGeom *dg,
+                        cudaStream_t st) {
     const int g = grid_for(N, kBlock, 1 << 20);
+    if constexpr (sizeof(T) == 4) {
+        if (nterms == 3) {
+            if (D == 2)
+                k_spread_runs<2><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
+            else
+                k_spread_runs<1><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
+            return cudaGetLastError();
+        }
+    }
     if (D == 2) {
-        if (gg.nterms == 3)
-            k_spread<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+        if (nterms == 3)
+            k_spread<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
         else
-            k_spread<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+            k_spread<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
     } else {
-        if (gg.nterms == 3)
-            k_spread<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+        if (nterms == 3)
+            k_spread<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
         else
-            k_spread<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, grid);
+            k_spread<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &gg, Cell4<T> *grid, cudaStream_t st) {
+    return spread_impl<T>(Y, N, D, gg.nterms, make_box(gg, (T *) nullptr), grid, nullptr, st);
+}
+
+template <typename T>
+cudaError_t launch_spread_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, Cell4<T> *grid,
+                              cudaStream_t st) {
+    BoxP<T> b{};
+    b.nterms = nterms;
+    return spread_impl<T>(Y, N, D, nterms, b, grid, dg, st);
+}
+
+template <typename T>
+cudaError_t gather_impl(const T *Y, int N, int D, int nterms, const BoxP<T> &b, const Cell4<T> *pot, int mode, T *rep,
+                        RedScratch r, const DevGeom *dg, cudaStream_t st) {
+    const int g = grid_for(N, kBlock, kRedGrid);
+    if (D == 2) {
+        if (nterms == 3)
+            k_gather<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
+        else
+            k_gather<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
+    } else {
+        if (nterms == 3)
+            k_gather<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
+        else
+            k_gather<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
     }
     return cudaGetLastError();
 }
@@ -727,45 +893,102 @@ cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &gg, Cell4<T>
 template <typename T>
 cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &gg, const Cell4<T> *pot, int mode, T *rep,
                           RedScratch r, cudaStream_t st) {
-    const BoxP<T> b = make_box(gg, (T *) nullptr);
-    const int g = grid_for(N, kBlock, kRedGrid);
-    if (D == 2) {
-        if (gg.nterms == 3)
-            k_gather<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
-        else
-            k_gather<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
-    } else {
-        if (gg.nterms == 3)
-            k_gather<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
-        else
-            k_gather<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r);
+    return gather_impl<T>(Y, N, D, gg.nterms, make_box(gg, (T *) nullptr), pot, mode, rep, r, nullptr, st);
+}
+
+template <typename T>
+cudaError_t launch_gather_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, const Cell4<T> *pot, int mode,
+                              T *rep, RedScratch r, cudaStream_t st) {
+    BoxP<T> b{};
+    b.nterms = nterms;
+    return gather_impl<T>(Y, N, D, nterms, b, pot, mode, rep, r, dg, st);
+}
+
+namespace {
+// Sizes the grid of this iteration from the min / max that k_center_minmax left in r.mnmx
+// (the host rule of make_grid_geom, in the same FP64 operations) and ORs its status into
+// *status_acc.  A grid above the capacity is clamped to it so that every kernel stays in
+// its buffers; the iteration is then void and the caller repeats it with a larger one.
+__global__ void k_geometry(RedScratch r, int D, int nterms, double ipi, int min_num, int nb_cap, int L_cap,
+                           DevGeom *__restrict__ dg, int *__restrict__ status_acc) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double mn = r.mnmx[0], mx = r.mnmx[1];
+    int status = 0;
+    if (!isfinite(mn) || !isfinite(mx)) {
+        status = 2;
+        mn = 0.0;
+        mx = 1.0;
     }
+    int clamped = 0;
+    GridGeom g = grid_geom(mn, mx, D, nterms, ipi, min_num, nb_cap, &clamped);
+    int L = smooth_even_at_least(2 * g.M);
+    if (clamped || L > L_cap) {
+        status = status ? status : 1;
+        while (L > L_cap && g.nb > 1) {  // shrink until it fits (results void anyway)
+            g = grid_geom(mn, mx, D, nterms, ipi, min_num, g.nb - 1, &clamped);
+            L = smooth_even_at_least(2 * g.M);
+        }
+    }
+    dg->g = g;
+    dg->conv.M = g.M;
+    dg->conv.h = g.hk;
+    make_fft_plan(L, &dg->conv.plan);
+    dg->status = status;
+    if (status) atomicOr(status_acc, status == 2 ? 2 : 1);
+}
+}  // namespace
+
+cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min_num, int nb_cap, int L_cap,
+                            DevGeom *dg, int *status_acc, cudaStream_t st) {
+    k_geometry<<<1, 32, 0, st>>>(r, D, nterms, ipi, min_num, nb_cap, L_cap, dg, status_acc);
     return cudaGetLastError();
+}
+
+template <typename T, int D, int G, int U, bool B = false>
+cudaError_t attr_launch(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout, T *uY,
+                        T *gains, T *dC, const T *rep, int N, const UpdateParams &p, RedScratch r, cudaStream_t st) {
+    // one resident wave: the warps take row groups from a counter
+    static int wave = 0;
+    if (wave == 0) {
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, D, G, U, B>, kBlock, 0);
+        if (e != cudaSuccess) return e;
+        wave = std::min(kMaxRedBlocks, nsm * (per_sm > 0 ? per_sm : 1));
+    }
+    const int g = grid_for(((long long) N + 31) / 32 * 32, kBlock, wave);
+    k_attr<T, D, G, U, B><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
+    return cudaGetLastError();
+}
+
+template <typename T, int D>
+cudaError_t attr_dispatch(int shape, const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
+                          T *uY, T *gains, T *dC, const T *rep, int N, const UpdateParams &p, RedScratch r,
+                          cudaStream_t st) {
+    switch (shape) {
+        case 1: return attr_launch<T, D, 32, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        case 2: return attr_launch<T, D, 8, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        case 3: return attr_launch<T, D, 16, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        case 4: return attr_launch<T, D, 32, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        case 5: return attr_launch<T, D, 16, 4, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        default: return attr_launch<T, D, 16, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+    }
 }
 
 template <typename T>
 cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
                                T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
-                               RedScratch r, cudaStream_t st) {
-    // one resident wave: the warps take row groups from a counter
-    static int wave[2] = {0, 0};
-    int &w = wave[D == 2 ? 1 : 0];
-    if (w == 0) {
-        int dev = 0, nsm = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaError_t e = (D == 2) ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, 2>, kBlock, 0)
-                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, 1>, kBlock, 0);
-        if (e != cudaSuccess) return e;
-        w = nsm * (per_sm > 0 ? per_sm : 1);
-        if (w > kMaxRedBlocks) w = kMaxRedBlocks;
-    }
-    const int g = grid_for(((long long) N + 31) / 32 * 32, kBlock, w);
-    if (D == 2)
-        k_attr<T, 2><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
-    else
-        k_attr<T, 1><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
-    return cudaGetLastError();
+                               RedScratch r, cudaStream_t st, int shape) {
+    if (D == 2) return attr_dispatch<T, 2>(shape, row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+    return attr_dispatch<T, 1>(shape, row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+}
+
+int attr_shape_info(int shape, int *group, int *unroll) {
+    if (shape < 0 || shape >= kNumAttrShapes) return -1;
+    *group = kAttrShapes[shape][0];
+    *unroll = kAttrShapes[shape][1];
+    return 0;
 }
 
 template <typename T>
@@ -811,9 +1034,13 @@ cudaError_t launch_cast_from_double(const double *src, T *dst, size_t n, cudaStr
     template cudaError_t launch_spread<T>(const T *, int, int, const GridGeom &, Cell4<T> *, cudaStream_t);     \
     template cudaError_t launch_gather<T>(const T *, int, int, const GridGeom &, const Cell4<T> *, int, T *,     \
                                           RedScratch, cudaStream_t);                                            \
+    template cudaError_t launch_gather_dev<T>(const T *, int, int, int, const DevGeom *, const Cell4<T> *, int,  \
+                                              T *, RedScratch, cudaStream_t);                                   \
+    template cudaError_t launch_spread_dev<T>(const T *, int, int, int, const DevGeom *, Cell4<T> *,            \
+                                              cudaStream_t);                                                    \
     template cudaError_t launch_attr_update<T>(const uint32_t *, const uint32_t *, const T *, const T *, T *,    \
                                                T *, T *, T *, const T *, int, int, const UpdateParams &,         \
-                                               RedScratch, cudaStream_t);                                       \
+                                               RedScratch, cudaStream_t, int);                                  \
     template cudaError_t launch_kl<T>(const uint32_t *, const uint32_t *, const T *, const T *, int, int, double, \
                                       double, RedScratch, cudaStream_t);                                        \
     template cudaError_t launch_y_from_double<T>(const double *, T *, int, int, cudaStream_t);                  \

@@ -40,6 +40,69 @@ struct GridGeom {
     double s64[kMaxInterp], inv_den64[kMaxInterp];
 };
 
+// The reference's grid rule (computeFftGradient*, tsne.cpp:769-780, 1039-1077; box bounds
+// and node positions of n_body_fft_2d / nbodyfft): box count truncated from the extent,
+// rounded up to the FFT-friendly list below 200 in 2-D; nodes at (k + 1/2) / nterms of a
+// box.  Host and device compute it with the same FP64 operations.  A box count above
+// nb_max is clamped to nb_max and reported through *clamped (capacity of a captured grid).
+FITSNE_HD GridGeom grid_geom(double mn, double mx, int D, int nterms, double ipi, int min_num, int nb_max,
+                             int *clamped) {
+    GridGeom g;
+    int nb = static_cast<int>(fmax((double) min_num, (mx - mn) / ipi));
+    if (D == 2) {
+        const int allowed[20] = {25, 36, 50, 55, 60, 65, 70, 75, 80, 85, 90, 96, 100, 110, 120, 130, 140, 150, 175, 200};
+        if (nb < allowed[19]) {
+            int i = 0;
+            while (allowed[i] < nb) ++i;
+            nb = allowed[i];
+        }
+    }
+    if (nb < 1) nb = 1;
+    if (clamped) *clamped = 0;
+    if (nb > nb_max) {
+        nb = nb_max;
+        if (clamped) *clamped = 1;
+    }
+    g.nb = nb;
+    g.nterms = nterms;
+    g.M = nb * nterms;
+    const double bw = (mx - mn) / (double) nb;
+    // n_body_fft_2d / nbodyfft read the lower corner and the width back from the box
+    // bounds array: lower[0] = 0*bw + mn, width = (1*bw + mn) - (0*bw + mn)
+    g.mn = 0.0 * bw + mn;
+    g.bw = (1.0 * bw + mn) - g.mn;
+    g.hk = bw / (double) nterms;
+    const double h = 1.0 / (double) nterms;
+    double s[kMaxInterp];
+    s[0] = h / 2.0;
+    for (int i = 1; i < nterms && i < kMaxInterp; ++i) s[i] = s[i - 1] + h;
+    for (int i = 0; i < kMaxInterp; ++i) {
+        g.s64[i] = 0.0;
+        g.inv_den64[i] = 0.0;
+        g.s32[i] = 0.f;
+        g.inv_den32[i] = 0.f;
+    }
+    for (int i = 0; i < nterms && i < kMaxInterp; ++i) {
+        double den = 1.0;
+        for (int j = 0; j < nterms; ++j)
+            if (i != j) den *= s[i] - s[j];
+        g.s64[i] = s[i];
+        g.inv_den64[i] = 1.0 / den;
+        g.s32[i] = (float) s[i];
+        g.inv_den32[i] = (float) (1.0 / den);
+    }
+    return g;
+}
+
+// Geometry of one iteration in device memory (see ConvGeom).  status: 0 ok, 1 the grid
+// exceeded the capacity it was launched for (results of the iteration are void), 2 the
+// coordinates are not finite.
+struct DevGeom {
+    GridGeom g;
+    ConvGeom conv;
+    int status;
+};
+
 // Reduction scratch shared by the kernels of one embedding (device memory).
 struct RedScratch {
     double *part;          // per-block partials, up to kMaxRedBlocks * 4 doubles
@@ -71,10 +134,24 @@ cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &g, Cell4<T> 
 template <typename T>
 cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &g, const Cell4<T> *pot, int mode, T *rep,
                           RedScratch r, cudaStream_t st);
+// As launch_spread / launch_gather with the geometry read from device memory.
+template <typename T>
+cudaError_t launch_spread_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, Cell4<T> *grid,
+                              cudaStream_t st);
+template <typename T>
+cudaError_t launch_gather_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, const Cell4<T> *pot, int mode,
+                              T *rep, RedScratch r, cudaStream_t st);
+// Grid of the current iteration from r.mnmx into dg (see k_geometry in grad.cu).
+cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min_num, int nb_cap, int L_cap,
+                            DevGeom *dg, int *status_acc, cudaStream_t st);
+// Number of attraction launch shapes (rows per work item x edges per lane; see grad.cu) and
+// the shape of an index.
+constexpr int kNumAttrShapes = 6;
+int attr_shape_info(int shape, int *group, int *unroll);
 template <typename T>
 cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
                                T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
-                               RedScratch r, cudaStream_t st);
+                               RedScratch r, cudaStream_t st, int shape = 0);
 template <typename T>
 cudaError_t launch_kl(const uint32_t *row, const uint32_t *col, const T *val, const T *Y, int N, int D, double exag,
                       double df, RedScratch r, cudaStream_t st);

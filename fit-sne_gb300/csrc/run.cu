@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -144,6 +145,144 @@ int optimise(const DevCSR &P, double *Y, int N, int no_dims, const GridParams &g
     if (!rc) rc = emb.run_schedule(s, 0, s.max_iter, costs, vb);
     if (!rc) rc = emb.get_Y(Y);
     if (rc) return set_error(rc == -13 ? FITSNE_E_GRID : FITSNE_E_CUDA, emb.error());
+    return 0;
+}
+
+// Batched form: independent embeddings advanced together, one CUDA graph per chunk with
+// one branch per job (fork / join through events onto the jobs' streams), so that the
+// small per-iteration kernels of all jobs run side by side.  Shared schedule and grid
+// parameters; per-job data, perplexity and learning rate.
+struct BatchJob {
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+    Embedding<float> emb;
+};
+
+int batch_iterate(std::vector<std::unique_ptr<BatchJob>> &jobs, const Schedule &s, const std::vector<double> &lr,
+                  double *const *costs, cudaStream_t master, double *stats) {
+    const int nj = (int) jobs.size();
+    double mult = s.early_exag_coeff, momentum = s.momentum;
+    auto params = [&](int it, int j) {
+        UpdateParams p{};
+        p.mode = 1;
+        p.exag = mult;
+        p.momentum = momentum;
+        p.learning_rate = lr[j];
+        p.df = 1.0;
+        p.use_gains = 1;
+        p.max_step_norm = s.max_step_norm;
+        (void) it;
+        return p;
+    };
+    auto kl_due = [&](int it) { return (it + 1) % 50 == 0 || it == s.max_iter - 1; };
+    auto after = [&](int it) -> int {
+        if (it == s.stop_lying_iter) mult /= s.early_exag_coeff;
+        if (it == s.mom_switch_iter) momentum = s.final_momentum;
+        if (kl_due(it))
+            for (int j = 0; j < nj; ++j) {
+                double C = 0.0;
+                if (jobs[j]->emb.kl(mult, &C)) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
+                if (it < s.stop_lying_iter && s.stop_lying_iter != -1)
+                    C = C / s.early_exag_coeff - std::log(s.early_exag_coeff);
+                if (costs && costs[j]) costs[j][it] = C;
+            }
+        return 0;
+    };
+    if (s.max_iter <= 0) return 0;
+    // first iteration on the host path (grid sizes, launch shapes)
+    for (int j = 0; j < nj; ++j) {
+        if (jobs[j]->emb.step(params(0, j), true)) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
+        jobs[j]->emb.set_first_geometry();
+    }
+    int rc = after(0);
+    if (rc) return rc;
+    cudaEvent_t fork = nullptr;
+    if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess)
+        return set_error(FITSNE_E_CUDA, "event");
+    cudaGraphExec_t exec = nullptr;
+    std::vector<unsigned long long> key_cached;
+    double launches = 0, captures = 0, redo = 0;
+    int it = 1;
+    while (it < s.max_iter) {
+        for (int j = 0; j < nj; ++j)
+            if (jobs[j]->emb.reorder_due(it, 0) && jobs[j]->emb.reorder_now())
+                return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
+        int end = it + 1;
+        auto reorder_any = [&](int i) {
+            for (auto &jb : jobs)
+                if (jb->emb.reorder_due(i, 0)) return true;
+            return false;
+        };
+        while (end < s.max_iter &&
+               !(kl_due(end - 1) || end - 1 == s.stop_lying_iter || end - 1 == s.mom_switch_iter || reorder_any(end)))
+            ++end;
+        const int len = end - it;
+        std::vector<unsigned long long> key;
+        std::vector<bool> am(nj);
+        for (int j = 0; j < nj; ++j) {
+            if (jobs[j]->emb.plan_capacity(0)) return set_error(FITSNE_E_GRID, jobs[j]->emb.error());
+            am[j] = jobs[j]->emb.mean_pending();
+            std::vector<unsigned long long> k = jobs[j]->emb.chunk_key(params(it, j), len);
+            key.insert(key.end(), k.begin(), k.end());
+        }
+        if (!exec || key != key_cached) {
+            if (exec) cudaGraphExecDestroy(exec);
+            exec = nullptr;
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(master, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+                return set_error(FITSNE_E_CUDA, "batch capture");
+            cudaEventRecord(fork, master);
+            int rr = 0;
+            for (int j = 0; j < nj && !rr; ++j) {
+                cudaStreamWaitEvent(jobs[j]->st, fork, 0);
+                rr = jobs[j]->emb.record_chunk(params(it, j), len, am[j]);
+                cudaEventRecord(jobs[j]->done, jobs[j]->st);
+                cudaStreamWaitEvent(master, jobs[j]->done, 0);
+            }
+            cudaError_t ce = cudaStreamEndCapture(master, &g);
+            if (!rr && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (rr || ce != cudaSuccess) return set_error(FITSNE_E_CUDA, "batch graph: " + std::string(cudaGetErrorString(ce)));
+            key_cached = key;
+            captures += 1;
+        }
+        if (cudaGraphLaunch(exec, master) != cudaSuccess || cudaStreamSynchronize(master) != cudaSuccess)
+            return set_error(FITSNE_E_CUDA, "batch graph launch");
+        launches += 1;
+        for (int j = 0; j < nj; ++j) {
+            int r = jobs[j]->emb.finish_chunk(len);
+            while (r == 1) {  // this job outgrew its grid: redo its chunk alone with more room
+                redo += 1;
+                Embedding<float> &e = jobs[j]->emb;
+                if (e.plan_capacity(1)) return set_error(FITSNE_E_GRID, e.error());
+                cudaGraph_t g = nullptr;
+                cudaGraphExec_t x = nullptr;
+                cudaStreamBeginCapture(jobs[j]->st, cudaStreamCaptureModeRelaxed);
+                int rr = e.record_chunk(params(it, j), len, am[j]);
+                cudaError_t ce = cudaStreamEndCapture(jobs[j]->st, &g);
+                if (!rr && ce == cudaSuccess) ce = cudaGraphInstantiate(&x, g, 0);
+                if (g) cudaGraphDestroy(g);
+                if (!rr && ce == cudaSuccess) ce = cudaGraphLaunch(x, jobs[j]->st);
+                if (!rr && ce == cudaSuccess) ce = cudaStreamSynchronize(jobs[j]->st);
+                if (x) cudaGraphExecDestroy(x);
+                if (rr || ce != cudaSuccess) return set_error(FITSNE_E_CUDA, "batch redo");
+                r = e.finish_chunk(len);
+            }
+            if (r < 0) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
+        }
+        for (int k = it; k < end; ++k) {
+            rc = after(k);
+            if (rc) return rc;
+        }
+        it = end;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    cudaEventDestroy(fork);
+    if (stats) {
+        stats[2] = launches;
+        stats[3] = captures;
+        stats[4] = redo;
+    }
     return 0;
 }
 
@@ -465,6 +604,87 @@ int fitsne_symmetrize(unsigned int **row_P, unsigned int **col_P, double **val_P
     *row_P = r;
     *col_P = c;
     *val_P = v;
+    return 0;
+}
+
+int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int *D, double *const *Y, int no_dims,
+                     const double *perplexity, const double *learning_rate, const int *rand_seed,
+                     int skip_random_init, int max_iter, int stop_lying_iter, int mom_switch_iter, double momentum,
+                     double final_momentum, double early_exag_coeff, int nterms, double intervals_per_integer,
+                     int min_num_intervals, double max_step_norm, double *const *costs, double *stats5) {
+    if (njobs < 1 || !X || !N || !D || !Y || !perplexity || !learning_rate)
+        return set_error(FITSNE_E_ARG, "invalid batch arguments");
+    if (no_dims != 1 && no_dims != 2)
+        return set_error(FITSNE_E_ARG, "FFT interpolation scheme supports only 1 or 2 output dimensions");
+    if (nterms < 1 || nterms > kMaxInterp || !(intervals_per_integer > 0) || min_num_intervals < 1)
+        return set_error(FITSNE_E_ARG, "invalid interpolation grid parameters");
+    for (int j = 0; j < njobs; ++j) {
+        if (!X[j] || !Y[j] || N[j] < 2 || D[j] < 1 || !(perplexity[j] > 0))
+            return set_error(FITSNE_E_ARG, "invalid data arguments of job " + std::to_string(j));
+        if (N[j] - 1 < 3 * perplexity[j])
+            return set_error(FITSNE_E_ARG, "Perplexity too large for the number of data points!");
+    }
+    int rc = check_cuda_device();
+    if (rc) return rc;
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::unique_ptr<BatchJob>> jobs;
+    for (int j = 0; j < njobs; ++j) {
+        jobs.emplace_back(new BatchJob());
+        if (cudaStreamCreateWithFlags(&jobs[j]->st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&jobs[j]->done, cudaEventDisableTiming) != cudaSuccess)
+            return set_error(FITSNE_E_CUDA, "stream / event creation failed");
+    }
+    struct Cleanup {
+        std::vector<std::unique_ptr<BatchJob>> &v;
+        ~Cleanup() {
+            for (auto &j : v) {
+                cudaStream_t st = j->st;
+                cudaEvent_t ev = j->done;
+                j.reset();
+                if (ev) cudaEventDestroy(ev);
+                if (st) cudaStreamDestroy(st);
+            }
+        }
+    } cleanup{jobs};
+    GridParams gp;
+    gp.nterms = nterms;
+    gp.intervals_per_integer = intervals_per_integer;
+    gp.min_num_intervals = min_num_intervals;
+    gp.df = 1.0;
+    // similarities and initial embeddings, job by job
+    for (int j = 0; j < njobs; ++j) {
+        DevCSR P;
+        rc = build_P(X[j], N[j], D[j], perplexity[j], -1, -1.0, 0, nullptr, &P, jobs[j]->st, false, false);
+        if (rc) return rc;
+        if (!skip_random_init) {
+            std::srand(rand_seed ? (unsigned int) rand_seed[j] : 0u);
+            for (size_t i = 0; i < (size_t) N[j] * no_dims; ++i) Y[j][i] = randn_polar() * .0001;
+        }
+        rc = jobs[j]->emb.init_device(N[j], no_dims, P.row, P.col, P.val, P.nnz, Y[j], gp, jobs[j]->st);
+        free_csr(P);
+        if (rc) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    Schedule s;
+    s.max_iter = max_iter;
+    s.stop_lying_iter = stop_lying_iter;
+    s.mom_switch_iter = mom_switch_iter;
+    s.momentum = momentum;
+    s.final_momentum = final_momentum;
+    s.early_exag_coeff = early_exag_coeff;
+    s.max_step_norm = max_step_norm;
+    std::vector<double> lr(learning_rate, learning_rate + njobs);
+    Stream master;
+    double st5[5] = {0, 0, 0, 0, 0};
+    rc = batch_iterate(jobs, s, lr, costs, master.s, st5);
+    if (rc) return rc;
+    for (int j = 0; j < njobs; ++j)
+        if (jobs[j]->emb.get_Y(Y[j])) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
+    const auto t2 = std::chrono::steady_clock::now();
+    st5[0] = std::chrono::duration<double>(t1 - t0).count();
+    st5[1] = std::chrono::duration<double>(t2 - t1).count();
+    if (stats5)
+        for (int k = 0; k < 5; ++k) stats5[k] = st5[k];
     return 0;
 }
 

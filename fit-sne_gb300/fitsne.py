@@ -18,6 +18,7 @@ BIN_PATH = os.path.join(HERE, "bin", "fast_tsne")
 
 _u32p = ctypes.POINTER(ctypes.c_uint)
 _f64p = ctypes.POINTER(ctypes.c_double)
+_f32p = ctypes.POINTER(ctypes.c_float)
 _i32p = ctypes.POINTER(ctypes.c_int)
 _lib = None
 
@@ -67,6 +68,16 @@ _SIGS = {
                                                    ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                    ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                                    _f64p, ctypes.c_void_p]),
+    "fitsne_batch_run": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_f64p), _i32p, _i32p, ctypes.POINTER(_f64p),
+                                        ctypes.c_int, _f64p, _f64p, _i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_f64p), _f64p]),
+    "fitsne_set_calibration": (None, [ctypes.c_int]),
+    "fitsne_get_calibration": (ctypes.c_int, []),
+    "fitsne_calibration_stats": (ctypes.c_int, [_f64p]),
+    "fitsne_mlp_param_count": (ctypes.c_int, [ctypes.c_int]),
+    "fitsne_mlp_loss_grad": (ctypes.c_int, [_f32p, ctypes.c_int, _f64p, _f64p, ctypes.c_int, ctypes.c_double,
+                                            ctypes.c_double, _f32p, _f64p]),
     "fitsne_set_precision": (None, [ctypes.c_int]),
     "fitsne_get_precision": (ctypes.c_int, []),
     "fitsne_last_error": (ctypes.c_char_p, []),
@@ -128,6 +139,73 @@ def set_precision(bits: int) -> None:
 
 def get_precision() -> int:
     return int(lib().fitsne_get_precision())
+
+
+def batch_run(Xs, perplexities, learning_rates=None, Y0s=None, seeds=None, no_dims=2, max_iter=1000,
+              stop_lying_iter=250, mom_switch_iter=250, momentum=0.5, final_momentum=0.8, early_exag_coeff=12.0,
+              nterms=3, intervals_per_integer=1.0, min_num_intervals=50, max_step_norm=5.0):
+    """Batched form: independent embeddings advanced together (fitsne_batch_run).
+    Returns (list of Y, list of costs, stats dict)."""
+    nj = len(Xs)
+    Xs = [np.ascontiguousarray(X, dtype=np.float64) for X in Xs]
+    N = np.array([X.shape[0] for X in Xs], dtype=np.int32)
+    D = np.array([X.shape[1] for X in Xs], dtype=np.int32)
+    perp = np.ascontiguousarray(perplexities, dtype=np.float64)
+    lr = np.ascontiguousarray(learning_rates if learning_rates is not None else [max(200.0, n / 12.0) for n in N],
+                              dtype=np.float64)
+    skip = Y0s is not None
+    Ys = [np.ascontiguousarray(Y0s[j], dtype=np.float64).reshape(N[j], no_dims).copy() if skip
+          else np.zeros((N[j], no_dims)) for j in range(nj)]
+    sd = np.ascontiguousarray(seeds if seeds is not None else np.arange(nj), dtype=np.int32)
+    costs = [np.zeros(max(1, max_iter)) for _ in range(nj)]
+    xp = (_f64p * nj)(*[_p(X, _f64p) for X in Xs])
+    yp = (_f64p * nj)(*[_p(Y, _f64p) for Y in Ys])
+    cp = (_f64p * nj)(*[_p(c, _f64p) for c in costs])
+    stats = np.zeros(5)
+    _check(lib().fitsne_batch_run(nj, xp, _p(N, _i32p), _p(D, _i32p), yp, no_dims, _p(perp, _f64p), _p(lr, _f64p),
+                                  _p(sd, _i32p), int(skip), max_iter, stop_lying_iter, mom_switch_iter, momentum,
+                                  final_momentum, early_exag_coeff, nterms, intervals_per_integer, min_num_intervals,
+                                  max_step_norm, cp, _p(stats, _f64p)))
+    keys = ["similarity_s", "iterate_s", "graph_launches", "graph_captures", "chunks_redone"]
+    return Ys, costs, dict(zip(keys, stats.tolist()))
+
+
+def set_calibration(mode) -> None:
+    """"bisection" (0, the reference's; default) or "learned" (1, MLP warm start) for the
+    similarity stage's perplexity calibration."""
+    m = {"bisection": 0, "learned": 1}.get(mode, mode)
+    lib().fitsne_set_calibration(int(m))
+
+
+def get_calibration() -> str:
+    return "learned" if lib().fitsne_get_calibration() == 1 else "bisection"
+
+
+def calibration_stats() -> dict:
+    """Statistics of the last calibration (see fitsne_calibration_stats in the header)."""
+    out = np.zeros(12)
+    _check(lib().fitsne_calibration_stats(out.ctypes.data_as(_f64p)))
+    keys = ["rows", "rows_harvest", "rows_fallback", "train_steps", "evals_plain", "evals_warm", "loss_first",
+            "loss_last", "ms_harvest", "ms_train", "ms_infer", "ms_warm"]
+    return dict(zip(keys, out.tolist()))
+
+
+def mlp_param_count(K: int) -> int:
+    return int(lib().fitsne_mlp_param_count(int(K)))
+
+
+def mlp_loss_grad(params, dist, beta, mu=0.0, sd=1.0):
+    """(loss, grad) of the calibration network on the GPU for the rows of dist (nrows x K)."""
+    dist = np.ascontiguousarray(dist, dtype=np.float64)
+    beta = np.ascontiguousarray(beta, dtype=np.float64)
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    nrows, K = dist.shape
+    grad = np.zeros_like(params)
+    loss = np.zeros(1)
+    _check(lib().fitsne_mlp_loss_grad(params.ctypes.data_as(_f32p), K, dist.ctypes.data_as(_f64p),
+                                      beta.ctypes.data_as(_f64p), nrows, float(mu), float(sd),
+                                      grad.ctypes.data_as(_f32p), loss.ctypes.data_as(_f64p)))
+    return float(loss[0]), grad
 
 
 def fft_gradient(row_P, col_P, val_P, Y, nterms=3, intervals_per_integer=1.0, min_num_intervals=50, df=1.0):

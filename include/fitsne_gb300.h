@@ -175,6 +175,56 @@ int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const unsigned int 
                                 void *stream);
 
 /* ---------------------------------------------------------------------------------
+ * Batched form (no reference counterpart; each job is what TSNE::run, src/tsne.cpp:118-
+ * 577, does for one data set, FP32 form, FFT gradient, df = 1, exact kNN).  njobs
+ * independent embeddings of any sizes: job j has HOST X[j] (N[j] x D[j]), Y[j] (N[j] x
+ * no_dims, in/out; initialised by libc srand(rand_seed[j]) + the polar method x 1e-4 unless
+ * skip_random_init), perplexity[j] (K = 3 perplexity) and learning_rate[j]; the schedule
+ * and grid arguments are shared.  The similarity stage runs job after job; the iterations
+ * advance all jobs together in chunks between the schedule's events, each chunk one CUDA
+ * graph with one branch per job, the grids sized on the device.  costs[j] (may be NULL, or
+ * costs itself) receives job j's KL every 50 iterations as in TSNE::run.  stats5 (may be
+ * NULL): seconds of the similarity stage, seconds of the iterations, chunk graph launches,
+ * graph captures, chunks repeated because a job's grid outgrew its capacity. */
+int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int *D, double *const *Y, int no_dims,
+                     const double *perplexity, const double *learning_rate, const int *rand_seed,
+                     int skip_random_init, int max_iter, int stop_lying_iter, int mom_switch_iter, double momentum,
+                     double final_momentum, double early_exag_coeff, int nterms, double intervals_per_integer,
+                     int min_num_intervals, double max_step_norm, double *const *costs, double *stats5);
+
+/* ---------------------------------------------------------------------------------
+ * Learned warm start of the perplexity calibration (no reference counterpart: the
+ * bisection it seeds is distances2similarities, src/tsne.cpp:1394-1469).
+ *
+ * fitsne_set_calibration(1) makes the similarity stage (fitsne_run, fitsne_gaussian_
+ * perplexity, fitsne_session_create_from_data) calibrate single-perplexity runs of at
+ * least 20,000 points as follows:
+ *   - the plain bisection (the reference's) on the first max(10000, min(N/10, 200000)) rows;
+ *   - training, on the GPU, of an MLP (K -> 64 -> 64 -> 1) that maps the row's scaled
+ *     kNN distances to log(beta * mean distance);
+ *   - for the other rows, a safeguarded Newton search from the predicted beta, to
+ *     |H - log(perplexity)| < 1e-6.
+ * 0 (default, or FITSNE_CALIBRATION unset / "bisection") keeps the reference's bisection
+ * everywhere: P is then identical to the reference's.  Perplexity lists and fixed sigma
+ * always use the bisection. */
+void fitsne_set_calibration(int mode);
+int fitsne_get_calibration(void);
+/* Statistics of this process's last calibration, out[12]: rows, harvested rows (plain
+ * bisection), predicted rows that needed bisection steps, training steps, mean entropy
+ * evaluations per harvested row, mean per predicted row, first and last training loss
+ * (standardised MSE), ms for harvest, training, inference, warm-started search.  Returns 0. */
+int fitsne_calibration_stats(double *out12);
+/* Number of FP32 parameters of the network for K distances per row: W1[64][K], b1[64],
+ * W2[64][64], b2[64], w3[64], b3. */
+int fitsne_mlp_param_count(int K);
+/* The network's loss and gradient on the GPU, for checking the training kernels: mean over
+ * the nrows rows (HOST dist[nrows*K] ascending, beta[nrows]) of (out - t)^2 with the target
+ * t = (log(beta * mean(dist)) - mu) / sd and input dist / mean(dist); params and grad are
+ * HOST arrays of fitsne_mlp_param_count(K) floats. */
+int fitsne_mlp_loss_grad(const float *params, int K, const double *dist, const double *beta, int nrows, double mu,
+                         double sd, float *grad, double *loss);
+
+/* ---------------------------------------------------------------------------------
  * Misc. */
 void fitsne_set_precision(int bits);
 int fitsne_get_precision(void);

@@ -8,7 +8,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "fit-sne_gb300")
 ORACLE = os.path.join(ROOT, "oracle")
-for p in (PKG, ORACLE, ROOT):
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+for p in (PKG, ORACLE, ROOT, GOLDEN):
     if p not in sys.path:
         sys.path.insert(0, p)
 
