@@ -291,16 +291,24 @@ def run_gb300(args, world, rank, local):
     s64.close()
     fp64_value = k64 / (fp64_ms / 1e3)
 
-    s32.set_timing(True)
+    # timed steps on the production path (graph-captured chunks, no per-iteration host
+    # round trip), then a short run with per-stage events (host path) for the stage split
+    s32.set_timing(False)
     s32.run(STEP_IT0, STEP_IT0 + args.warmup, **sched)
     barrier(world)
+    it_a = STEP_IT0 + args.warmup
+    it_b = it_a + args.steps
     with ClockSampler(local) as clk:
         t1 = time.perf_counter()
-        s32.run(STEP_IT0 + args.warmup, STEP_IT0 + args.warmup + args.steps, **sched)
+        s32.run(it_a, it_b, **sched)
         wall = time.perf_counter() - t1
+    run_ms = reduce_max(s32.stage_times()[8], world)
+    launches = int(s32.stage_times()[9])
+    s32.set_timing(True)
+    k_st = max(10, min(args.steps, 60))
+    s32.run(it_b, it_b + k_st, **sched)
     st = s32.stage_times()
     s32.close()
-    run_ms = reduce_max(st[8], world)
     value = world * args.steps / (run_ms / 1e3)
     attr_ms = st[4]
     abytes = attraction_bytes(N, nnz)
@@ -354,12 +362,15 @@ def run_gb300(args, world, rank, local):
                          "traffic": ATTR_TRAFFIC_RATIO * abytes, "bytes_per_launch": abytes,
                          "ms_per_launch": attr_ms},
             "stage_ms": {"centre_minmax": st[0], "spread": st[1], "fft_conv": st[2], "gather": st[3],
-                         "attraction_update": st[4], "iteration": st[5], "boxes_per_dim": st[6], "fft_len": st[7]},
+                         "attraction_update": st[4], "iteration": st[5], "boxes_per_dim": st[6], "fft_len": st[7],
+                         "note": "per-stage CUDA events over %d further steps on the host path (one min/max round "
+                                 "trip per iteration, inside the spread stage); value and ms_per_step are the "
+                                 "graph-captured production path" % k_st},
             "nnz": nnz, "wall_ms_per_step": 1e3 * wall / args.steps, "setup_s": setup_s,
             "state_extent": float(np.abs(Yburn).max()),
             "plain_fp64": {"value": fp64_value, "unit": "iters/s", "steps": k64, "speedup": value / fp64_value},
             "grad_rel_l2_vs_fp64": grad_rel, "Z": z32,
-            "gpu_launches": int(st[9]), "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e}
+            "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e}
     print(json.dumps(line))
     return 0
 

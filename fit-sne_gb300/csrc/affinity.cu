@@ -435,9 +435,10 @@ int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double per
             std::fprintf(stderr,
                          "[fitsne] calibration (learned warm start): %.3f s; %d harvested rows, %.1f evaluations "
                          "per row; %d training steps, loss %.3g -> %.3g; %d predicted rows, %.2f evaluations per "
-                         "row, %d with bisection steps\n",
+                         "row, %d with bisection steps; ms harvest %.1f, train %.1f, infer %.1f, search %.1f\n",
                          now_s() - t1, ms.rows_harvest, ms.iters_plain, ms.train_steps, ms.loss_first, ms.loss_last,
-                         ms.rows - ms.rows_harvest, ms.iters_warm, ms.rows_fallback);
+                         ms.rows - ms.rows_harvest, ms.iters_warm, ms.rows_fallback, ms.ms_harvest, ms.ms_train,
+                         ms.ms_infer, ms.ms_warm);
     } else {
         std::vector<int> evals;
         rc = calibrate_rows(dist, K + 1, 1, P.val, N, K, perplexity, sigma, list_len, list_host, nullptr, st, err,

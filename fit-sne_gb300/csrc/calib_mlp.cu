@@ -436,8 +436,8 @@ int calibrate_rows_learned(const double *dist, int stride, int offset, double *P
     MCK(cudaMemsetAsync(v, 0, sizeof(float) * o.n, st));
     MCK(cudaMemsetAsync(loss, 0, sizeof(double), st));
     MCK(cudaMemsetAsync(step, 0, sizeof(unsigned), st));
-    // about 8 passes over the harvest, at least 1000 and at most 3000 steps
-    const int nsteps = std::max(1000, std::min(3000, 8 * nh / kBatch)) / kGraphSteps * kGraphSteps;
+    // 1200 steps of 256: the search only needs a seed within a few per cent of beta
+    const int nsteps = 1200 / kGraphSteps * kGraphSteps;
     MCK(b.get(&hist, (size_t) nsteps));
     const size_t gsm = grad_smem(K);
     MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) gsm));

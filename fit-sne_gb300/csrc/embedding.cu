@@ -710,6 +710,37 @@ int Embedding<T>::finish_chunk(int len) {
 }
 
 template <typename T>
+int Embedding<T>::launch_chunk(const UpdateParams &p, int len, int grow) {
+    int rc = plan_capacity(grow);
+    if (rc) return rc;
+    const bool am = mean_pending_;
+    const std::vector<unsigned long long> key = chunk_key(p, len);
+    if (!gexec_ || key != gkey_) {
+        if (gexec_) {
+            cudaGraphExecDestroy(gexec_);
+            gexec_ = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        FITSNE_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeRelaxed));
+        rc = record_chunk(p, len, am);
+        cudaError_t ce = cudaStreamEndCapture(st_, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec_, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return fail("chunk graph", ce);
+        gkey_ = key;
+        ++captures_;
+    }
+    gchunk_cur0_ = cur_;
+    gchunk_len_ = len;
+    FITSNE_CK(cudaGraphLaunch(gexec_, st_));
+    return 0;
+}
+
+template <typename T>
 std::vector<unsigned long long> Embedding<T>::chunk_key(const UpdateParams &p, int len) const {
     std::vector<unsigned long long> key;
     auto put = [&key](const void *v, size_t n) {
@@ -802,40 +833,19 @@ int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, doubl
             int rr = reorder();
             if (rr) return rr;
         }
+        // chunks of at most kMaxChunk iterations, so that the grid capacity follows the
+        // embedding's growth and a repeated chunk costs little
         int end = it + 1;
-        while (end < it1 && !(kl_due(end - 1) || end - 1 == s.stop_lying_iter || end - 1 == s.start_late_exag_iter ||
-                              end - 1 == s.mom_switch_iter || reorder_due(end)))
+        while (end < it1 && end - it < kMaxChunk &&
+               !(kl_due(end - 1) || end - 1 == s.stop_lying_iter || end - 1 == s.start_late_exag_iter ||
+                 end - 1 == s.mom_switch_iter || reorder_due(end)))
             ++end;
         const int len = end - it;
         const UpdateParams p = params(it);
         int grow = 0;
         while (true) {
-            int rc = plan_capacity(grow);
+            int rc = launch_chunk(p, len, grow);
             if (rc) return rc;
-            const bool am = mean_pending_;
-            const std::vector<unsigned long long> key = chunk_key(p, len);
-            if (!gexec_ || key != gkey_) {
-                if (gexec_) {
-                    cudaGraphExecDestroy(gexec_);
-                    gexec_ = nullptr;
-                }
-                cudaGraph_t graph = nullptr;
-                FITSNE_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeRelaxed));
-                rc = record_chunk(p, len, am);
-                cudaError_t ce = cudaStreamEndCapture(st_, &graph);
-                if (rc) {
-                    if (graph) cudaGraphDestroy(graph);
-                    return rc;
-                }
-                if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec_, graph, 0);
-                if (graph) cudaGraphDestroy(graph);
-                if (ce != cudaSuccess) return fail("chunk graph", ce);
-                gkey_ = key;
-                gchunk_cur0_ = cur_;
-                gchunk_len_ = len;
-            }
-            gchunk_cur0_ = cur_;
-            FITSNE_CK(cudaGraphLaunch(gexec_, st_));
             FITSNE_CK(cudaStreamSynchronize(st_));
             rc = finish_chunk(len);
             if (rc < 0) return rc;

@@ -32,6 +32,8 @@ struct Schedule {
 
 // Embeddings smaller than this are not renumbered (they fit in cache either way).
 constexpr int kReorderMinN = 16384;
+// Longest run of iterations replayed as one CUDA graph.
+constexpr int kMaxChunk = 50;
 
 struct GridParams {
     int nterms = 3;
@@ -95,6 +97,10 @@ class Embedding {
     // Capacity for the next chunk from the last known box count (grows buffers; call
     // outside any capture).  grow > 0 forces a larger capacity after an overflow.
     int plan_capacity(int grow);
+    // plan_capacity + record (or reuse the cached graph of) a chunk on this object's stream
+    // and launch it without synchronising; finish_chunk after the stream is idle.
+    int launch_chunk(const UpdateParams &p, int len, int grow);
+    unsigned long long graph_captures() const { return captures_; }
     // Runs iterations [it0, it1) with graph chunks; costs may be null.
     int run_schedule_graphs(const Schedule &s, int it0, int it1, double *costs, bool verbose);
     // What a recorded chunk depends on (parameters, capacity, buffers): equal keys replay.
@@ -181,6 +187,7 @@ class Embedding {
     std::vector<unsigned long long> gkey_;
     int grid_buffers(int M, int L);    // grows grid / FFT buffers to M x M, L
     int gchunk_len_ = 0;
+    unsigned long long captures_ = 0;
     int gchunk_cur0_ = 0;
 
     // locality renumbering (reorder.cuh): perm_[k] = caller index of internal point k

@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ X
             const double nq = norms[q];
             // FP32 direct differences (SIMT scan) or BF16 hi/lo tensor-core products (knn_tc.cuh)
             const double eps =
-                tc ? 1.5 * (D + 4) * u * sC + 1e-4 * nq * maxnorm + 2e-5 * (nq * nq + maxnorm * maxnorm) + 1e-30
+                tc ? 1.5 * (D + 4) * u * sC + 3e-5 * nq * maxnorm + 4e-6 * (nq * nq + maxnorm * maxnorm) + 1e-30
                    : 1.5 * ((D + 4) * u * sC + 4.0 * u * sqrt(sC) * (nq + maxnorm)) + 1e-30;
             const double sK = ed[K - 1] * ed[K - 1];
             ok = (sK < sC - eps) ? 1 : 0;

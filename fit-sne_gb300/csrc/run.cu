@@ -148,18 +148,17 @@ int optimise(const DevCSR &P, double *Y, int N, int no_dims, const GridParams &g
     return 0;
 }
 
-// Batched form: independent embeddings advanced together, one CUDA graph per chunk with
-// one branch per job (fork / join through events onto the jobs' streams), so that the
-// small per-iteration kernels of all jobs run side by side.  Shared schedule and grid
-// parameters; per-job data, perplexity and learning rate.
+// Batched form: independent embeddings advanced together, chunk by chunk; each job's chunk is
+// one CUDA graph (cached per job) launched on the job's own stream, so that the small
+// per-iteration kernels of all jobs run side by side with one host synchronisation per job
+// and chunk.  Shared schedule and grid parameters; per-job data, perplexity and learning rate.
 struct BatchJob {
     cudaStream_t st = nullptr;
-    cudaEvent_t done = nullptr;
     Embedding<float> emb;
 };
 
 int batch_iterate(std::vector<std::unique_ptr<BatchJob>> &jobs, const Schedule &s, const std::vector<double> &lr,
-                  double *const *costs, cudaStream_t master, double *stats) {
+                  double *const *costs, double *stats) {
     const int nj = (int) jobs.size();
     double mult = s.early_exag_coeff, momentum = s.momentum;
     auto params = [&](int it, int j) {
@@ -196,11 +195,6 @@ int batch_iterate(std::vector<std::unique_ptr<BatchJob>> &jobs, const Schedule &
     }
     int rc = after(0);
     if (rc) return rc;
-    cudaEvent_t fork = nullptr;
-    if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess)
-        return set_error(FITSNE_E_CUDA, "event");
-    cudaGraphExec_t exec = nullptr;
-    std::vector<unsigned long long> key_cached;
     double launches = 0, captures = 0, redo = 0;
     int it = 1;
     while (it < s.max_iter) {
@@ -217,55 +211,21 @@ int batch_iterate(std::vector<std::unique_ptr<BatchJob>> &jobs, const Schedule &
                !(kl_due(end - 1) || end - 1 == s.stop_lying_iter || end - 1 == s.mom_switch_iter || reorder_any(end)))
             ++end;
         const int len = end - it;
-        std::vector<unsigned long long> key;
-        std::vector<bool> am(nj);
-        for (int j = 0; j < nj; ++j) {
-            if (jobs[j]->emb.plan_capacity(0)) return set_error(FITSNE_E_GRID, jobs[j]->emb.error());
-            am[j] = jobs[j]->emb.mean_pending();
-            std::vector<unsigned long long> k = jobs[j]->emb.chunk_key(params(it, j), len);
-            key.insert(key.end(), k.begin(), k.end());
-        }
-        if (!exec || key != key_cached) {
-            if (exec) cudaGraphExecDestroy(exec);
-            exec = nullptr;
-            cudaGraph_t g = nullptr;
-            if (cudaStreamBeginCapture(master, cudaStreamCaptureModeRelaxed) != cudaSuccess)
-                return set_error(FITSNE_E_CUDA, "batch capture");
-            cudaEventRecord(fork, master);
-            int rr = 0;
-            for (int j = 0; j < nj && !rr; ++j) {
-                cudaStreamWaitEvent(jobs[j]->st, fork, 0);
-                rr = jobs[j]->emb.record_chunk(params(it, j), len, am[j]);
-                cudaEventRecord(jobs[j]->done, jobs[j]->st);
-                cudaStreamWaitEvent(master, jobs[j]->done, 0);
-            }
-            cudaError_t ce = cudaStreamEndCapture(master, &g);
-            if (!rr && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
-            if (g) cudaGraphDestroy(g);
-            if (rr || ce != cudaSuccess) return set_error(FITSNE_E_CUDA, "batch graph: " + std::string(cudaGetErrorString(ce)));
-            key_cached = key;
-            captures += 1;
-        }
-        if (cudaGraphLaunch(exec, master) != cudaSuccess || cudaStreamSynchronize(master) != cudaSuccess)
-            return set_error(FITSNE_E_CUDA, "batch graph launch");
-        launches += 1;
+        // every job's chunk graph (cached per job, recaptured only when that job's key
+        // changes) launched on its own stream: the jobs' kernels run side by side
+        for (int j = 0; j < nj; ++j)
+            if (jobs[j]->emb.launch_chunk(params(it, j), len, 0))
+                return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
+        launches += nj;
+        for (int j = 0; j < nj; ++j)
+            if (cudaStreamSynchronize(jobs[j]->st) != cudaSuccess) return set_error(FITSNE_E_CUDA, "batch chunk");
         for (int j = 0; j < nj; ++j) {
             int r = jobs[j]->emb.finish_chunk(len);
-            while (r == 1) {  // this job outgrew its grid: redo its chunk alone with more room
+            while (r == 1) {  // this job outgrew its grid: its chunk again, with more room
                 redo += 1;
                 Embedding<float> &e = jobs[j]->emb;
-                if (e.plan_capacity(1)) return set_error(FITSNE_E_GRID, e.error());
-                cudaGraph_t g = nullptr;
-                cudaGraphExec_t x = nullptr;
-                cudaStreamBeginCapture(jobs[j]->st, cudaStreamCaptureModeRelaxed);
-                int rr = e.record_chunk(params(it, j), len, am[j]);
-                cudaError_t ce = cudaStreamEndCapture(jobs[j]->st, &g);
-                if (!rr && ce == cudaSuccess) ce = cudaGraphInstantiate(&x, g, 0);
-                if (g) cudaGraphDestroy(g);
-                if (!rr && ce == cudaSuccess) ce = cudaGraphLaunch(x, jobs[j]->st);
-                if (!rr && ce == cudaSuccess) ce = cudaStreamSynchronize(jobs[j]->st);
-                if (x) cudaGraphExecDestroy(x);
-                if (rr || ce != cudaSuccess) return set_error(FITSNE_E_CUDA, "batch redo");
+                if (e.launch_chunk(params(it, j), len, 1) || cudaStreamSynchronize(jobs[j]->st) != cudaSuccess)
+                    return set_error(FITSNE_E_CUDA, e.error());
                 r = e.finish_chunk(len);
             }
             if (r < 0) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
@@ -276,8 +236,7 @@ int batch_iterate(std::vector<std::unique_ptr<BatchJob>> &jobs, const Schedule &
         }
         it = end;
     }
-    if (exec) cudaGraphExecDestroy(exec);
-    cudaEventDestroy(fork);
+    for (auto &jb : jobs) captures += (double) jb->emb.graph_captures();
     if (stats) {
         stats[2] = launches;
         stats[3] = captures;
@@ -630,18 +589,15 @@ int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int 
     std::vector<std::unique_ptr<BatchJob>> jobs;
     for (int j = 0; j < njobs; ++j) {
         jobs.emplace_back(new BatchJob());
-        if (cudaStreamCreateWithFlags(&jobs[j]->st, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&jobs[j]->done, cudaEventDisableTiming) != cudaSuccess)
-            return set_error(FITSNE_E_CUDA, "stream / event creation failed");
+        if (cudaStreamCreateWithFlags(&jobs[j]->st, cudaStreamNonBlocking) != cudaSuccess)
+            return set_error(FITSNE_E_CUDA, "stream creation failed");
     }
     struct Cleanup {
         std::vector<std::unique_ptr<BatchJob>> &v;
         ~Cleanup() {
             for (auto &j : v) {
                 cudaStream_t st = j->st;
-                cudaEvent_t ev = j->done;
                 j.reset();
-                if (ev) cudaEventDestroy(ev);
                 if (st) cudaStreamDestroy(st);
             }
         }
@@ -674,9 +630,8 @@ int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int 
     s.early_exag_coeff = early_exag_coeff;
     s.max_step_norm = max_step_norm;
     std::vector<double> lr(learning_rate, learning_rate + njobs);
-    Stream master;
     double st5[5] = {0, 0, 0, 0, 0};
-    rc = batch_iterate(jobs, s, lr, costs, master.s, st5);
+    rc = batch_iterate(jobs, s, lr, costs, st5);
     if (rc) return rc;
     for (int j = 0; j < njobs; ++j)
         if (jobs[j]->emb.get_Y(Y[j])) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());

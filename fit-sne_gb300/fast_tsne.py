@@ -16,6 +16,7 @@ binary exit with an error.  PCA initialisation uses scikit-learn when it is inst
 from __future__ import annotations
 
 import os
+import sys
 import struct
 import subprocess
 from datetime import datetime
@@ -27,20 +28,19 @@ BINARY = os.path.join(os.path.dirname(os.path.realpath(__file__)), "bin", "fast_
 
 
 def _pca_init(X, map_dims, seed):
-    """First map_dims principal components, scaled to std 1e-4 on the first axis."""
-    try:
+    """First map_dims principal components, scaled to std 1e-4 on the first axis
+    (fast_tsne.py:186-197 of the reference).  Computed on the GPU (fitsne_pca: the
+    covariance's leading eigenvectors, each component's largest-magnitude entry positive,
+    as scikit-learn's PCA does); FITSNE_PCA=sklearn uses scikit-learn instead."""
+    if os.environ.get("FITSNE_PCA") == "sklearn":
         from sklearn.decomposition import PCA
         solver = "arpack" if X.shape[1] > map_dims else "auto"
         pca = PCA(n_components=map_dims, svd_solver=solver, random_state=seed if seed != -1 else None)
         init = pca.fit_transform(X)
-    except ImportError:
-        Xc = X - X.mean(axis=0)
-        U, S, _ = np.linalg.svd(Xc, full_matrices=False)
-        U = U[:, :map_dims]
-        # sign convention of scikit-learn's svd_flip: largest |u| of each column positive
-        signs = np.sign(U[np.argmax(np.abs(U), axis=0), np.arange(map_dims)])
-        signs[signs == 0] = 1.0
-        init = U * S[:map_dims] * signs
+    else:
+        sys.path.insert(0, os.path.dirname(os.path.realpath(__file__)))
+        import fitsne
+        init = fitsne.pca(X, map_dims)
     init = init / np.std(init[:, 0])
     return init * 0.0001
 

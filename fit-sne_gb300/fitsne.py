@@ -72,6 +72,7 @@ _SIGS = {
                                         ctypes.c_int, _f64p, _f64p, _i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_f64p), _f64p]),
+    "fitsne_pca": (ctypes.c_int, [_f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p]),
     "fitsne_set_calibration": (None, [ctypes.c_int]),
     "fitsne_get_calibration": (ctypes.c_int, []),
     "fitsne_calibration_stats": (ctypes.c_int, [_f64p]),
@@ -168,6 +169,15 @@ def batch_run(Xs, perplexities, learning_rates=None, Y0s=None, seeds=None, no_di
                                   max_step_norm, cp, _p(stats, _f64p)))
     keys = ["similarity_s", "iterate_s", "graph_launches", "graph_captures", "chunks_redone"]
     return Ys, costs, dict(zip(keys, stats.tolist()))
+
+
+def pca(X, n_components=2):
+    """First principal components of X on the GPU (fitsne_pca)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    N, D = X.shape
+    Y = np.zeros((N, n_components))
+    _check(lib().fitsne_pca(_p(X, _f64p), N, D, int(n_components), _p(Y, _f64p)))
+    return Y
 
 
 def set_calibration(mode) -> None:

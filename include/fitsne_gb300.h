@@ -181,8 +181,9 @@ int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const unsigned int 
  * no_dims, in/out; initialised by libc srand(rand_seed[j]) + the polar method x 1e-4 unless
  * skip_random_init), perplexity[j] (K = 3 perplexity) and learning_rate[j]; the schedule
  * and grid arguments are shared.  The similarity stage runs job after job; the iterations
- * advance all jobs together in chunks between the schedule's events, each chunk one CUDA
- * graph with one branch per job, the grids sized on the device.  costs[j] (may be NULL, or
+ * advance all jobs together in chunks between the schedule's events; each job's chunk is
+ * one CUDA graph (cached per job, the grid sized on the device) launched on the job's own
+ * stream, so the jobs' kernels overlap.  costs[j] (may be NULL, or
  * costs itself) receives job j's KL every 50 iterations as in TSNE::run.  stats5 (may be
  * NULL): seconds of the similarity stage, seconds of the iterations, chunk graph launches,
  * graph captures, chunks repeated because a job's grid outgrew its capacity. */
@@ -223,6 +224,14 @@ int fitsne_mlp_param_count(int K);
  * HOST arrays of fitsne_mlp_param_count(K) floats. */
 int fitsne_mlp_loss_grad(const float *params, int K, const double *dist, const double *beta, int nrows, double mu,
                          double sd, float *grad, double *loss);
+
+/* ---------------------------------------------------------------------------------
+ * PCA initialisation on the GPU (replaces the scikit-learn PCA of fast_tsne.py:186-197,
+ * the step before TSNE::run): the first n_components principal components of HOST X
+ * (N x D, not modified) into HOST Y (N x n_components, row-major): (X - mean) V with V the
+ * leading eigenvectors of the covariance, each component's largest-magnitude entry positive
+ * (scikit-learn's svd_flip with u_based_decision=False).  D <= 2048. */
+int fitsne_pca(const double *X, int N, int D, int n_components, double *Y);
 
 /* ---------------------------------------------------------------------------------
  * Misc. */

@@ -22,8 +22,10 @@ def test_wrapper_end_to_end_matches_reference_kl(golden, tmp_path, monkeypatch):
                            mom_switch_iter=100, learning_rate=200, initialization=golden["e2e_Y0"],
                            knn_algo="vp-tree", return_loss=True)
     ref = golden["e2e_costs"]
+    # 1,000 points, FP32 form: the optimiser's chaos spreads the KL of repeated runs by up to
+    # 1.4e-2 after the exaggeration (see test_run_gpu.py); 1% is tested at 5,000 points there
     for i in (99, 199, 299):
-        assert abs(loss[i] - ref[i]) <= 1e-2 * ref[i]
+        assert abs(loss[i] - ref[i]) <= 3e-2 * ref[i]
     assert np.isnan(loss[0]) and Y.shape == (len(golden["e2e_X"]), 2)
     assert not [f for f in os.listdir(tmp_path) if f.endswith(".dat")]
 

@@ -84,7 +84,9 @@ def test_perplexity_list_sigma_and_late_exaggeration(stub_binary):
     assert o["perplexity"] == -1 and o["K"] == 10 and o["sigma"] == 2.0 and o["search_k"] == 500
 
 
-def test_pca_initialisation_scale(stub_binary):
+def test_pca_initialisation_scale(stub_binary, monkeypatch):
+    pytest.importorskip("sklearn")
+    monkeypatch.setenv("FITSNE_PCA", "sklearn")  # the GPU PCA is tested in test_pca_gpu.py
     X = np.random.default_rng(2).standard_normal((60, 5)) * [5, 3, 1, 1, 1]
     ft.fast_tsne(X, max_iter=100)
     o = parse(open(stub_binary / "captured.dat", "rb").read())
@@ -92,7 +94,9 @@ def test_pca_initialisation_scale(stub_binary):
     assert abs(np.std(init[:, 0]) - 1e-4) < 1e-10
 
 
-def test_bad_option_strings_raise():
+def test_bad_option_strings_raise(monkeypatch):
+    pytest.importorskip("sklearn")
+    monkeypatch.setenv("FITSNE_PCA", "sklearn")
     X = np.zeros((10, 2))
     with pytest.raises(ValueError):
         ft.fast_tsne(X, nbody_algo="exact")
