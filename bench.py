@@ -466,7 +466,7 @@ def run_batch(args, world, rank):
                                    "perplexity 10/30/50 cycled, 2-D, df=1, %d iterations" % (len(jobs), sum(n), iters)},
             "batch_seconds": batch_s, "similarity_seconds": st["similarity_s"], "iterate_seconds": st["iterate_s"],
             "iterate_iters_per_s": len(jobs) * iters / st["iterate_s"], "graph_launches": st["graph_launches"],
-            "graph_captures": st["graph_captures"], "chunks_redone": st["chunks_redone"],
+            "graph_instantiations": st["graph_instantiations"], "chunks_redone": st["chunks_redone"],
             "one_by_one_seconds": single_s, "speedup_vs_one_by_one": single_s / batch_s,
             "max_final_kl_rel_dev_vs_one_by_one": kl_dev}
     print(json.dumps(line))

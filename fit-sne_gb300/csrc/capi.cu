@@ -205,6 +205,12 @@ int fitsne_session_set_timing(fitsne_session *s, int on) {
     return 0;
 }
 
+int fitsne_session_set_graphs(fitsne_session *s, int on) {
+    if (!s || !s->impl) return set_error(FITSNE_E_ARG, "null session");
+    s->impl->set_graphs(on != 0);
+    return 0;
+}
+
 int fitsne_session_stage_times(fitsne_session *s, double *out10) {
     if (!s || !s->impl || !out10) return set_error(FITSNE_E_ARG, "null argument");
     s->impl->times(out10);

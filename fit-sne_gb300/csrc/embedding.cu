@@ -716,10 +716,6 @@ int Embedding<T>::launch_chunk(const UpdateParams &p, int len, int grow) {
     const bool am = mean_pending_;
     const std::vector<unsigned long long> key = chunk_key(p, len);
     if (!gexec_ || key != gkey_) {
-        if (gexec_) {
-            cudaGraphExecDestroy(gexec_);
-            gexec_ = nullptr;
-        }
         cudaGraph_t graph = nullptr;
         FITSNE_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeRelaxed));
         rc = record_chunk(p, len, am);
@@ -728,11 +724,27 @@ int Embedding<T>::launch_chunk(const UpdateParams &p, int len, int grow) {
             if (graph) cudaGraphDestroy(graph);
             return rc;
         }
-        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec_, graph, 0);
+        // same topology (a new capacity, new buffers after a renumbering, new schedule
+        // parameters): update the instantiated graph in place, else instantiate anew
+        bool updated = false;
+        if (ce == cudaSuccess && gexec_ && gexec_len_ == len) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(gexec_, graph, &info) == cudaSuccess;
+            if (!updated) cudaGetLastError();  // clear the failed update
+        }
+        if (ce == cudaSuccess && !updated) {
+            if (gexec_) {
+                cudaGraphExecDestroy(gexec_);
+                gexec_ = nullptr;
+            }
+            ce = cudaGraphInstantiate(&gexec_, graph, 0);
+        }
         if (graph) cudaGraphDestroy(graph);
         if (ce != cudaSuccess) return fail("chunk graph", ce);
         gkey_ = key;
+        gexec_len_ = len;
         ++captures_;
+        if (updated) ++updates_;
     }
     gchunk_cur0_ = cur_;
     gchunk_len_ = len;

@@ -101,6 +101,7 @@ class Embedding {
     // and launch it without synchronising; finish_chunk after the stream is idle.
     int launch_chunk(const UpdateParams &p, int len, int grow);
     unsigned long long graph_captures() const { return captures_; }
+    unsigned long long graph_updates() const { return updates_; }
     // Runs iterations [it0, it1) with graph chunks; costs may be null.
     int run_schedule_graphs(const Schedule &s, int it0, int it1, double *costs, bool verbose);
     // What a recorded chunk depends on (parameters, capacity, buffers): equal keys replay.
@@ -187,7 +188,8 @@ class Embedding {
     std::vector<unsigned long long> gkey_;
     int grid_buffers(int M, int L);    // grows grid / FFT buffers to M x M, L
     int gchunk_len_ = 0;
-    unsigned long long captures_ = 0;
+    unsigned long long captures_ = 0, updates_ = 0;
+    int gexec_len_ = 0;  // chunk length of the instantiated graph
     int gchunk_cur0_ = 0;
 
     // locality renumbering (reorder.cuh): perm_[k] = caller index of internal point k

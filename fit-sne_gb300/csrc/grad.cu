@@ -12,8 +12,9 @@ constexpr int kRedGrid = 1216;  // 152 SMs x 8 resident blocks of 256 threads
 // Launch shapes of the attraction pass: consecutive rows per work item (<= 32) and CSR
 // edges per lane per batch.  Entry 0 is the default; Embedding's autotuner times the rest.
 // Shape 5: the 8 warps of a block take 8 consecutive groups at once, so that the neighbour
-// gathers of an SM's warps overlap in its L1.
-constexpr int kAttrShapes[kNumAttrShapes][2] = {{16, 4}, {32, 4}, {8, 4}, {16, 2}, {32, 2}, {16, 4}};
+// gathers of an SM's warps overlap in its L1.  Shape 6: a warp loads the next row's first
+// batch of CSR entries before it gathers the current row's neighbours.
+constexpr int kAttrShapes[kNumAttrShapes][2] = {{16, 4}, {32, 4}, {8, 4}, {16, 2}, {32, 2}, {16, 4}, {16, 4}};
 
 // ---------------------------------------------------------------------------------
 // storage layouts of Y
@@ -60,6 +61,11 @@ struct YL<double, 1> {
     static FITSNE_D void load(const double *Y, int i, P *c) { c[0] = __ldg(Y + i); }
     static FITSNE_D void store(double *Y, int i, const P *c) { Y[i] = c[0]; }
 };
+
+// 1 / x correctly rounded: the same value as the IEEE division 1.f / x, in fewer
+// instructions (the attraction evaluates it once per non-zero of P)
+FITSNE_D float recip(float x) { return __frcp_rn(x); }
+FITSNE_D double recip(double x) { return 1.0 / x; }
 
 FITSNE_D float pdiff(df32 a, df32 b) { return df_diff(a, b); }
 FITSNE_D double pdiff(double a, double b) { return a - b; }
@@ -554,7 +560,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 // remain: the CSR entries (prefetched into L2 while the previous row is processed) and the
 // neighbour Y gathers (L2-resident).  Within a row, lanes take kAttrUnroll edges each per
 // batch: all index / value loads first, then all gathers.
-template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups = false>
+template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups = false, bool kPipe = false>
 __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
                                                  const T *__restrict__ val, const T *__restrict__ Yin,
                                                  T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
@@ -611,8 +617,34 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
         T amy[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) amy[d] = T(0);
+        // one batch of kAttrUnroll edges per lane: CSR index and value, or (self, 0) past e1
+        auto load_batch = [&](uint32_t base, uint32_t e1, int self, uint32_t (&jj)[kAttrUnroll],
+                              T (&vv)[kAttrUnroll]) {
+#pragma unroll
+            for (int u = 0; u < kAttrUnroll; ++u) {
+                const uint32_t e = base + lane + 32 * u;
+                const bool ok = e < e1;
+                jj[u] = ok ? __ldcs(col + e) : (uint32_t) self;
+                vv[u] = ok ? __ldcs(val + e) : T(0);
+            }
+        };
+        // pipelined shape: the next row's first batch is loaded while this row gathers
+        uint32_t jn[kAttrUnroll];
+        T vn[kAttrUnroll];
+        if constexpr (kPipe) load_batch(__shfl_sync(full, rb, 0), __shfl_sync(full, re, 0), i0, jn, vn);
         for (int k = 0; k < nr; ++k) {
             const uint32_t e0 = __shfl_sync(full, rb, k), e1 = __shfl_sync(full, re, k);
+            uint32_t jc[kAttrUnroll];
+            T vc[kAttrUnroll];
+            if constexpr (kPipe) {
+#pragma unroll
+                for (int u = 0; u < kAttrUnroll; ++u) {
+                    jc[u] = jn[u];
+                    vc[u] = vn[u];
+                }
+                if (k + 1 < nr)
+                    load_batch(__shfl_sync(full, rb, k + 1), __shfl_sync(full, re, k + 1), i0 + k + 1, jn, vn);
+            }
             if (k + 1 < nr) {
                 // the next row's CSR lines into L2 (lanes 0-15 columns, 16-31 values)
                 const uint32_t f0 = __shfl_sync(full, rb, k + 1), f1 = __shfl_sync(full, re, k + 1);
@@ -642,12 +674,14 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
             for (uint32_t base = e0; base < e1; base += 32 * kAttrUnroll) {
                 uint32_t j[kAttrUnroll];
                 T v[kAttrUnroll];
+                if (kPipe && base == e0) {
 #pragma unroll
-                for (int u = 0; u < kAttrUnroll; ++u) {
-                    const uint32_t e = base + lane + 32 * u;
-                    const bool ok = e < e1;
-                    j[u] = ok ? __ldcs(col + e) : (uint32_t) i;
-                    v[u] = ok ? __ldcs(val + e) : T(0);
+                    for (int u = 0; u < kAttrUnroll; ++u) {
+                        j[u] = jc[u];
+                        v[u] = vc[u];
+                    }
+                } else {
+                    load_batch(base, e1, i, j, v);
                 }
                 P cj[kAttrUnroll][D];
 #pragma unroll
@@ -661,7 +695,7 @@ __global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ ro
                         dx[d] = pdiff(ci[d], cj[u][d]);
                         d2 += dx[d] * dx[d];
                     }
-                    const T q = df1 ? T(1) / (T(1) + d2) : T(1) / (T(1) + d2 / df);
+                    const T q = recip(df1 ? T(1) + d2 : T(1) + d2 / df);
                     const T vq = v[u] * q;
 #pragma unroll
                     for (int d = 0; d < D; ++d) a[d] += vq * dx[d];
@@ -944,7 +978,7 @@ cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min
     return cudaGetLastError();
 }
 
-template <typename T, int D, int G, int U, bool B = false>
+template <typename T, int D, int G, int U, bool B = false, bool PP = false>
 cudaError_t attr_launch(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout, T *uY,
                         T *gains, T *dC, const T *rep, int N, const UpdateParams &p, RedScratch r, cudaStream_t st) {
     // one resident wave: the warps take row groups from a counter
@@ -953,12 +987,12 @@ cudaError_t attr_launch(const uint32_t *row, const uint32_t *col, const T *val, 
         int dev = 0, nsm = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, D, G, U, B>, kBlock, 0);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, D, G, U, B, PP>, kBlock, 0);
         if (e != cudaSuccess) return e;
         wave = std::min(kMaxRedBlocks, nsm * (per_sm > 0 ? per_sm : 1));
     }
     const int g = grid_for(((long long) N + 31) / 32 * 32, kBlock, wave);
-    k_attr<T, D, G, U, B><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
+    k_attr<T, D, G, U, B, PP><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
     return cudaGetLastError();
 }
 
@@ -972,6 +1006,8 @@ cudaError_t attr_dispatch(int shape, const uint32_t *row, const uint32_t *col, c
         case 3: return attr_launch<T, D, 16, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
         case 4: return attr_launch<T, D, 32, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
         case 5: return attr_launch<T, D, 16, 4, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        case 6:
+            return attr_launch<T, D, 16, 4, false, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
         default: return attr_launch<T, D, 16, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
     }
 }

@@ -19,11 +19,13 @@
 //   warp 1      allocates 128 TMEM columns (two 128 x 64 FP32 accumulators) and issues
 //               the tcgen05.mma (M = 128, N = 64, K = 16) from one thread; tcgen05.commit
 //               releases the shared-memory stage and hands the accumulator to the epilogue
-//   warps 2..5  epilogue: tcgen05.ld of their 32 TMEM lanes (= 32 queries), threshold test
-//               into a per-thread bit mask; when a lane of the warp keeps a column, the chunk
-//               goes to a shared-memory stash and every lane walks its own mask into its
-//               per-query max-heap of the C best (shared memory), so the lanes' heap updates
-//               run side by side
+//   warps 2..5  epilogue: one tcgen05.ld of the whole 64-column tile for their 32 TMEM lanes
+//               (= 32 queries), after which the accumulator is handed back to the MMA warp;
+//               threshold test into per-thread bit masks (four independent chains per 32
+//               columns); when a lane of the warp keeps a column, the 32-column half goes to
+//               a shared-memory stash and every lane walks its own mask into its per-query
+//               max-heap of the C best (shared memory), so the lanes' heap updates run side by
+//               side and overlap the next MMAs
 // Every mbarrier wait gives up after about a second, sets an error flag, and the CTA
 // drains its own in-flight work, frees TMEM and returns.
 #include <cuda.h>
@@ -130,15 +132,21 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+// 64 consecutive columns of this warp's 32 lanes; the wait is part of the statement
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
-        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,"
+        "%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
           "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]),
+          "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
+          "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
+          "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
+          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
         : "r"(taddr)
         : "memory");
 }
@@ -325,23 +333,40 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (!(ok = __all_sync(0xffffffffu, mbar_wait(&bar_acc_full[b], phb, &abort_flag)))) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t tbase = tmem + ((uint32_t) (quarter * 32) << 16) + (uint32_t) (b * BN);
-#pragma unroll 1
-                for (int c0 = 0; c0 < BN; c0 += 32) {
-                    uint32_t v[32];
-                    tmem_ld32(tbase + (uint32_t) c0, v);
-                    const int colbase = ((t0 + t) % nRT) * BN + c0;
-                    const int nvalid = N - colbase;
-                    const uint32_t lim = nvalid >= 32 ? 0xffffffffu : (nvalid <= 0 ? 0u : ((1u << nvalid) - 1u));
-                    uint32_t mask = 0;
+                // the whole 64-column tile in one load; the accumulator goes back to the MMA
+                // warp at once, so the next MMAs overlap this tile's threshold test and inserts
+                uint32_t v[BN];
+                tmem_ld64(tbase, v);
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&bar_acc_empty[b]);
+                const int tilebase = ((t0 + t) % nRT) * BN;
+                const int nvalid = N - tilebase;
+                // kept-candidate masks, built in four independent chains per 32 columns
+                uint32_t mk[2];
 #pragma unroll
-                    for (int jj = 0; jj < 32; ++jj)
-                        mask |= (fmaf(-2.f, __uint_as_float(v[jj]), nq) < thr) ? (1u << jj) : 0u;
-                    mask &= lim;
+                for (int h = 0; h < 2; ++h) {
+                    uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+#pragma unroll
+                    for (int jj = 0; jj < 32; jj += 4) {
+                        q0 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj]), nq) < thr) ? (1u << jj) : 0u;
+                        q1 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj + 1]), nq) < thr) ? (2u << jj) : 0u;
+                        q2 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj + 2]), nq) < thr) ? (4u << jj) : 0u;
+                        q3 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj + 3]), nq) < thr) ? (8u << jj) : 0u;
+                    }
+                    const int nv = nvalid - 32 * h;
+                    const uint32_t lim = nv >= 32 ? 0xffffffffu : (nv <= 0 ? 0u : ((1u << nv) - 1u));
+                    mk[h] = ((q0 | q1) | (q2 | q3)) & lim;
+                }
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    uint32_t mask = mk[h];
                     if (__any_sync(0xffffffffu, mask != 0u)) {
-                        // stash the chunk (entry jj of row r at jj*BM + r: conflict-free), then
-                        // each lane inserts its own kept columns
+                        // stash the half (entry jj of row r at jj*BM + r: conflict-free), then each
+                        // lane inserts its own kept columns
 #pragma unroll
-                        for (int jj = 0; jj < 32; ++jj) my_stash[jj * BM] = __uint_as_float(v[jj]);
+                        for (int jj = 0; jj < 32; ++jj) my_stash[jj * BM] = __uint_as_float(v[32 * h + jj]);
+                        const int colbase = tilebase + 32 * h;
                         while (mask) {
                             const int jj = __ffs(mask) - 1;
                             mask &= mask - 1;
@@ -359,9 +384,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                         __syncwarp();
                     }
                 }
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&bar_acc_empty[b]);
             }
             if (!ok) break;
             if (qvalid) {

@@ -236,10 +236,14 @@ int batch_iterate(std::vector<std::unique_ptr<BatchJob>> &jobs, const Schedule &
         }
         it = end;
     }
-    for (auto &jb : jobs) captures += (double) jb->emb.graph_captures();
+    double updates = 0;
+    for (auto &jb : jobs) {
+        captures += (double) jb->emb.graph_captures();
+        updates += (double) jb->emb.graph_updates();
+    }
     if (stats) {
         stats[2] = launches;
-        stats[3] = captures;
+        stats[3] = captures - updates;  // instantiations (the rest were in-place updates)
         stats[4] = redo;
     }
     return 0;

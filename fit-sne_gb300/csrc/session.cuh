@@ -14,6 +14,7 @@ struct SessionBase {
     virtual int gradient(double *dC, double *sum_Q) = 0;
     virtual int get_y(double *Y) = 0;
     virtual void set_timing(bool on) = 0;
+    virtual void set_graphs(bool on) = 0;
     virtual void times(double *out10) = 0;
     virtual std::string error() = 0;
     cudaStream_t st = nullptr;
@@ -28,6 +29,7 @@ struct SessionT : SessionBase {
     int gradient(double *dC, double *sum_Q) override { return emb.gradient(dC, sum_Q); }
     int get_y(double *Y) override { return emb.get_Y(Y); }
     void set_timing(bool on) override { emb.set_timing(on); }
+    void set_graphs(bool on) override { emb.set_graphs(on); }
     void times(double *o) override {
         const StageTimes &t = emb.last_times();
         o[0] = t.center;

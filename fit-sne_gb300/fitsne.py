@@ -62,6 +62,7 @@ _SIGS = {
     "fitsne_session_gradient": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p]),
     "fitsne_session_get_y": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
     "fitsne_session_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fitsne_session_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fitsne_session_stage_times": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
     "fitsne_session_destroy": (None, [ctypes.c_void_p]),
     "fitsne_fft_gradient_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -167,7 +168,7 @@ def batch_run(Xs, perplexities, learning_rates=None, Y0s=None, seeds=None, no_di
                                   _p(sd, _i32p), int(skip), max_iter, stop_lying_iter, mom_switch_iter, momentum,
                                   final_momentum, early_exag_coeff, nterms, intervals_per_integer, min_num_intervals,
                                   max_step_norm, cp, _p(stats, _f64p)))
-    keys = ["similarity_s", "iterate_s", "graph_launches", "graph_captures", "chunks_redone"]
+    keys = ["similarity_s", "iterate_s", "graph_launches", "graph_instantiations", "chunks_redone"]
     return Ys, costs, dict(zip(keys, stats.tolist()))
 
 
@@ -410,6 +411,9 @@ class Session:
 
     def set_timing(self, on=True):
         _check(lib().fitsne_session_set_timing(self._h, int(bool(on))))
+
+    def set_graphs(self, on=True):
+        _check(lib().fitsne_session_set_graphs(self._h, int(bool(on))))
 
     def stage_times(self):
         out = np.zeros(10)

