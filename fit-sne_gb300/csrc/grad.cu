@@ -13,8 +13,11 @@ constexpr int kRedGrid = 1216;  // 152 SMs x 8 resident blocks of 256 threads
 // edges per lane per batch.  Entry 0 is the default; Embedding's autotuner times the rest.
 // Shape 5: the 8 warps of a block take 8 consecutive groups at once, so that the neighbour
 // gathers of an SM's warps overlap in its L1.  Shape 6: a warp loads the next row's first
-// batch of CSR entries before it gathers the current row's neighbours.
-constexpr int kAttrShapes[kNumAttrShapes][2] = {{16, 4}, {32, 4}, {8, 4}, {16, 2}, {32, 2}, {16, 4}, {16, 4}};
+// batch of CSR entries before it gathers the current row's neighbours.  Shapes 7, 8: registers
+// capped for 6 resident blocks (48 warps) per SM.  Shape 9: 160-edge batches (a typical row in
+// one batch).
+constexpr int kAttrShapes[kNumAttrShapes][2] = {{16, 4}, {32, 4}, {8, 4}, {16, 2}, {32, 2},
+                                                {16, 4}, {16, 4}, {16, 4}, {8, 4},  {16, 5}};
 
 // ---------------------------------------------------------------------------------
 // storage layouts of Y
@@ -560,8 +563,9 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 // remain: the CSR entries (prefetched into L2 while the previous row is processed) and the
 // neighbour Y gathers (L2-resident).  Within a row, lanes take kAttrUnroll edges each per
 // batch: all index / value loads first, then all gathers.
-template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups = false, bool kPipe = false>
-__global__ void __launch_bounds__(kBlock) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups = false, bool kPipe = false,
+          int kMinBlocks = 1>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
                                                  const T *__restrict__ val, const T *__restrict__ Yin,
                                                  T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
                                                  T *__restrict__ dC, const T *__restrict__ rep, int N,
@@ -978,7 +982,7 @@ cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min
     return cudaGetLastError();
 }
 
-template <typename T, int D, int G, int U, bool B = false, bool PP = false>
+template <typename T, int D, int G, int U, bool B = false, bool PP = false, int MB = 1>
 cudaError_t attr_launch(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout, T *uY,
                         T *gains, T *dC, const T *rep, int N, const UpdateParams &p, RedScratch r, cudaStream_t st) {
     // one resident wave: the warps take row groups from a counter
@@ -987,12 +991,13 @@ cudaError_t attr_launch(const uint32_t *row, const uint32_t *col, const T *val, 
         int dev = 0, nsm = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, D, G, U, B, PP>, kBlock, 0);
+        cudaError_t e =
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_attr<T, D, G, U, B, PP, MB>, kBlock, 0);
         if (e != cudaSuccess) return e;
         wave = std::min(kMaxRedBlocks, nsm * (per_sm > 0 ? per_sm : 1));
     }
     const int g = grid_for(((long long) N + 31) / 32 * 32, kBlock, wave);
-    k_attr<T, D, G, U, B, PP><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
+    k_attr<T, D, G, U, B, PP, MB><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
     return cudaGetLastError();
 }
 
@@ -1008,6 +1013,13 @@ cudaError_t attr_dispatch(int shape, const uint32_t *row, const uint32_t *col, c
         case 5: return attr_launch<T, D, 16, 4, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
         case 6:
             return attr_launch<T, D, 16, 4, false, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        case 7:
+            return attr_launch<T, D, 16, 4, false, false, 6>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r,
+                                                            st);
+        case 8:
+            return attr_launch<T, D, 8, 4, false, false, 6>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r,
+                                                           st);
+        case 9: return attr_launch<T, D, 16, 5>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
         default: return attr_launch<T, D, 16, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
     }
 }

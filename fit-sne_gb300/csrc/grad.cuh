@@ -146,7 +146,7 @@ cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min
                             DevGeom *dg, int *status_acc, cudaStream_t st);
 // Number of attraction launch shapes (rows per work item x edges per lane; see grad.cu) and
 // the shape of an index.
-constexpr int kNumAttrShapes = 7;
+constexpr int kNumAttrShapes = 10;
 int attr_shape_info(int shape, int *group, int *unroll);
 template <typename T>
 cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
