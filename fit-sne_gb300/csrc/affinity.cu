@@ -405,12 +405,7 @@ int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double per
     const bool tm = timing_requested();
     const double t0 = now_s();
     int rc = knn_exact(Xd, N, D, K + 1, idx, dist, st, &ks, &kerr);
-    if (tm)
-        std::fprintf(stderr,
-                     "[fitsne] kNN (K=%d, %s): %.3f s (candidates %.3f s, first pass %.3f s, rescans %.3f s), "
-                     "rows rescanned %d, unverified %d\n",
-                     K + 1, ks.tensor_cores ? "tcgen05 candidates" : "FP32 candidates", now_s() - t0,
-                     ks.s_candidates, ks.s_first_pass, ks.s_rescans, ks.rows_rescanned, ks.rows_unverified);
+    if (tm) print_knn_stats(K + 1, ks, now_s() - t0);
     if (rc) {
         err = kerr ? kerr : "kNN failed";
         cudaFree(idx);

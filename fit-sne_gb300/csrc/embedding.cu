@@ -547,8 +547,12 @@ int Embedding<T>::tune_attr() {
         }
     }
     const char *e = std::getenv("FITSNE_AUTOTUNE");
+    const char *fixed = std::getenv("FITSNE_ATTR_SHAPE");  // a fixed shape index, no tuning
     int best = 0;
-    if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
+    if (fixed && *fixed) {
+        best = std::atoi(fixed);
+        if (best < 0 || best >= kNumAttrShapes) best = 0;
+    } else if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
         UpdateParams p{};
         p.mode = 0;
         p.exag = 1.0;
@@ -582,8 +586,8 @@ int Embedding<T>::tune_attr() {
         if (timing_requested()) {
             int g = 0, u = 0;
             attr_shape_info(best, &g, &u);
-            std::fprintf(stderr, "[fitsne] attraction launch shape (N=%d, nnz=%zu%s): %d rows per work item, %d edges "
-                                 "per lane\n", N_, nnz_, reordered_ ? ", renumbered" : "", g, u);
+            std::fprintf(stderr, "[fitsne] attraction launch shape %d (N=%d, nnz=%zu%s): %d rows per work item, %d "
+                                 "edges per lane\n", best, N_, nnz_, reordered_ ? ", renumbered" : "", g, u);
         }
     }
     {

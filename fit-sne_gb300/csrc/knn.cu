@@ -1,6 +1,7 @@
 // Exact kNN: FP32 candidate scan + FP64 re-rank with verification (see knn.cuh).
 #include <cfloat>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <chrono>
 #include <string>
@@ -336,6 +337,20 @@ int pow2_at_least(int n) {
 
 }  // namespace
 
+void print_knn_stats(int K, const KnnStats &ks, double total_s) {
+    char tot[32] = "";
+    if (total_s >= 0) std::snprintf(tot, sizeof tot, "%.3f s, ", total_s);
+    std::fprintf(stderr,
+                 "[fitsne] kNN (K=%d, %s): %scandidates %.3f s, first pass %.3f s, rescans %.3f s, rows rescanned %d, "
+                 "unverified %d",
+                 K, ks.tensor_cores ? "tcgen05 candidates" : "FP32 candidates", tot, ks.s_candidates, ks.s_first_pass,
+                 ks.s_rescans, ks.rows_rescanned, ks.rows_unverified);
+    if (ks.tensor_cores)
+        std::fprintf(stderr, ", locality order %.3f s, tile pairs computed %.1f%%, per query %.0f columns kept, %.0f inserts",
+                     ks.tc.s_order, 100.0 * ks.tc.tiles_kept, ks.tc.cols_per_query, ks.tc.inserts_per_query);
+    std::fprintf(stderr, "\n");
+}
+
 int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist, cudaStream_t st, KnnStats *stats,
               const char **err) {
     static thread_local std::string msg;
@@ -402,7 +417,7 @@ int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist
         KCK(cudaMalloc(&cd, sizeof(float) * (size_t) N * C));
         KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) N * C));
         std::string terr;
-        if (knn_candidates_tc(Xd, N, D, C, cd, ci, st, terr) != 0) {
+        if (knn_candidates_tc(Xd, N, D, C, maxnorm, cd, ci, st, stats ? &stats->tc : nullptr, terr) != 0) {
             msg = terr;
             if (err) *err = msg.c_str();
             cudaFree(Xf);

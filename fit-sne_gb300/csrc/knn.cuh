@@ -15,6 +15,8 @@
 
 #include <cuda_runtime.h>
 
+#include "knn_tc.cuh"
+
 namespace fitsne {
 
 struct KnnStats {
@@ -24,7 +26,12 @@ struct KnnStats {
     double s_candidates = 0;   // host-clock seconds: first-pass candidates (tensor-core path)
     double s_first_pass = 0;   // first pass including the re-rank
     double s_rescans = 0;      // rescans of the unverified rows
+    KnnTcStats tc;             // tensor-core pass: tiles computed, inserts, ordering time
 };
+
+// One line of the timing report (FITSNE_TIMING): "[fitsne] kNN (K=..., path): ..."; total_s < 0
+// leaves the total out.
+void print_knn_stats(int K, const KnnStats &ks, double total_s);
 
 // Xd: N x D FP64 (device).  Writes idx[N*K] and dist[N*K] (device, FP64 non-squared,
 // ascending).  K includes the point itself (the reference asks for K + 1 neighbours).

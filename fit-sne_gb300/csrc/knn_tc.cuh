@@ -11,6 +11,13 @@ namespace fitsne {
 // Longest candidate list the shared-memory heaps of the tensor-core kernel hold.
 constexpr int kMaxTcCandidates = 120;
 
+struct KnnTcStats {
+    double tiles_kept = 1.0;         // fraction of (query tile, reference tile) pairs computed
+    double cols_per_query = 0;       // columns that passed a query's threshold test, per query
+    double inserts_per_query = 0;    // heap insertions (fills and replacements) per query
+    double s_order = 0;              // host-clock seconds of the locality order
+};
+
 // True when the device is a Blackwell (cc 10.x) part, the driver exposes the tensor-map
 // encoder, D <= 62 (two spare columns of the 64-wide operand rows) and C <= kMaxTcCandidates.
 bool knn_tc_supported(int D, int C);
@@ -23,7 +30,25 @@ bool knn_tc_supported(int D, int C);
 // 3 * 2^-18 |x||y| in the product (2.3e-5 |x||y| in d2); the accumulation adds at most
 // sixteen FP32 roundings (truncating or not) of partial sums below |x||y| + |y|^2 / 2
 // (< 2e-6 (|x||y| + |y|^2)).
-int knn_candidates_tc(const double *Xd, int N, int D, int C, float *cand_d, uint32_t *cand_i, cudaStream_t st,
-                      std::string &err);
+//
+// Reference tiles (64 points) that cannot hold a candidate of any query of a query tile (128
+// points) are skipped: their bounding spheres bound d^2 from below, and a tile is skipped when
+// that bound, less the error bound above (maxnorm = the largest |x|), exceeds the largest
+// current C-th distance of the tile's queries.  Superblocks of tiles are visited nearest
+// first, so the thresholds fall early and the walk stops at the first superblock too far
+// away.  The points are first put in a locality order (cells of the nearest of ~N/1024
+// sampled pivots, cells grouped by 32 super-pivots; FITSNE_KNN_ORDER=input keeps the
+// caller's order): the lists do not depend on the order, the skipping does.  stats may be
+// null.
+//
+// Exactness: a skipped point would not have entered the list had its tile been computed (its
+// approximate d^2 is above the threshold then in force, and thresholds only fall), so the
+// lists are the ones the full scan keeps, up to the order of equal approximate distances.
+int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, float *cand_d, uint32_t *cand_i,
+                      cudaStream_t st, KnnTcStats *stats, std::string &err);
+
+// 1: locality order before the candidate search (default), 0: the caller's order
+// (FITSNE_KNN_ORDER=input).
+int knn_order_mode();
 
 }  // namespace fitsne

@@ -433,12 +433,7 @@ int fitsne_knn(const double *X, int N, int D, int K, unsigned int *indices, doub
     if (e == cudaSuccess) {
         KnnStats ks;
         rc = knn_exact(Xd, N, D, K, idx, dist, st.s, &ks, &kerr);
-        if (!rc && timing_requested())
-            std::fprintf(stderr,
-                         "[fitsne] kNN (K=%d, %s): candidates %.3f s, first pass %.3f s, rescans %.3f s, "
-                         "rows rescanned %d, unverified %d\n",
-                         K, ks.tensor_cores ? "tcgen05 candidates" : "FP32 candidates", ks.s_candidates,
-                         ks.s_first_pass, ks.s_rescans, ks.rows_rescanned, ks.rows_unverified);
+        if (!rc && timing_requested()) print_knn_stats(K, ks, -1.0);
         if (!rc) {
             e = cudaMemcpyAsync(indices, idx, sizeof(uint32_t) * (size_t) N * K, cudaMemcpyDeviceToHost, st.s);
             if (e == cudaSuccess)

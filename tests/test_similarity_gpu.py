@@ -38,22 +38,39 @@ def test_knn_is_exact_against_bruteforce(gpu_lib, orc, N, D, K):
         assert set(idx[r][dist[r] < odist[r][-1]]) == set(oidx[r][odist[r] < odist[r][-1]])
 
 
-@pytest.mark.parametrize("N,D,K,spread,path", [(3001, 50, 91, 4.0, "tcgen05"), (4096, 62, 31, 0.3, "tcgen05"),
-                                                (1500, 20, 100, 2.0, "FP32"), (2000, 63, 20, 1.0, "FP32"),
-                                                (70001, 50, 91, 3.0, "tcgen05")])
-def test_tensor_core_candidates_give_the_exact_lists(gpu_lib, monkeypatch, capfd, N, D, K, spread, path):
-    """The tcgen05 candidate search (BF16 hi/lo split, folded norms) and the FP32 scan must
-    end in the same exact neighbour lists after the FP64 re-rank; tight clusters exercise the
-    rescans, N = 70001 a ragged last tile of a multi-tile grid.  K + 29 > 120 candidates or
-    D > 62 take the FP32 scan."""
+@pytest.mark.parametrize("N,D,K,spread,path,order", [(3001, 50, 91, 4.0, "tcgen05", "random"),
+                                                      (4096, 62, 31, 0.3, "tcgen05", "random"),
+                                                      (1500, 20, 100, 2.0, "FP32", "random"),
+                                                      (2000, 63, 20, 1.0, "FP32", "random"),
+                                                      (70001, 50, 91, 3.0, "tcgen05", "random"),
+                                                      (70001, 50, 91, 3.0, "tcgen05", "input"),
+                                                      (50001, 40, 91, 3.0, "tcgen05", "clusters"),
+                                                      (30000, 50, 31, 0.6, "tcgen05", "clusters")])
+def test_tensor_core_candidates_give_the_exact_lists(gpu_lib, monkeypatch, capfd, N, D, K, spread, path, order):
+    """The tcgen05 candidate search (BF16 hi/lo split, folded norms, tile skipping, locality
+    order) and the FP32 scan must end in the same exact neighbour lists after the FP64
+    re-rank; tight clusters exercise the rescans, N = 70001 a ragged last tile of a multi-tile
+    grid, well separated clusters the skipping of reference tiles, whether the rows come in
+    random order (put in locality order first) or grouped by cluster; "input" keeps the
+    caller's random order (FITSNE_KNN_ORDER=input).  K + 29 > 120 candidates or D > 62 take
+    the FP32 scan."""
     rng = np.random.default_rng(N + D)
     centres = rng.standard_normal((8, D)) * spread
-    X = centres[rng.integers(0, 8, N)] + rng.standard_normal((N, D)) * 0.05
+    lab = rng.integers(0, 8, N)
+    if order == "clusters":
+        lab = np.sort(lab)
+    if order == "input":
+        monkeypatch.setenv("FITSNE_KNN_ORDER", "input")
+    X = centres[lab] + rng.standard_normal((N, D)) * 0.05
     X = (X - X.mean(0)) / np.abs(X - X.mean(0)).max()
     monkeypatch.setenv("FITSNE_TIMING", "1")
     capfd.readouterr()
     idx_tc, d_tc = gpu_lib.knn(X, K)
-    assert path + " candidates" in capfd.readouterr().err
+    log = capfd.readouterr().err
+    assert path + " candidates" in log
+    if N >= 16384 and path == "tcgen05":  # 8 separated clusters: most reference tiles skipped
+        computed = float(log.split("tile pairs computed ")[1].split("%")[0])
+        assert (computed > 90.0) if order == "input" else (computed < 50.0), log
     monkeypatch.setenv("FITSNE_KNN", "simt")
     idx_s, d_s = gpu_lib.knn(X, K)
     assert np.allclose(d_tc, d_s, rtol=0, atol=0)
