@@ -28,8 +28,8 @@
 //               threshold test into per-thread bit masks (four independent chains per 32
 //               columns); when a lane of the warp keeps a column, the 32-column half goes to
 //               a shared-memory stash and every lane walks its own mask into its per-query
-//               max-heap of the C best (shared memory), so the lanes' heap updates run side by
-//               side and overlap the next MMAs
+//               4-ary max-heap of the C best (shared memory, knn_heap.cuh), so the lanes'
+//               heap updates run side by side and overlap the next MMAs
 // Every mbarrier wait gives up after about a second, sets an error flag, and the CTA
 // drains its own in-flight work, frees TMEM and returns.
 #include <cuda.h>
@@ -41,6 +41,7 @@
 #include <cstdlib>
 #include <string>
 
+#include "knn_heap.cuh"
 #include "knn_tc.cuh"
 #include "sort.cuh"
 
@@ -184,41 +185,6 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
         : "memory");
 }
 
-// per-thread max-heap of (distance, index) in shared memory, entry e of row `r` at e*BM + r
-struct Heap {
-    float *d;
-    uint32_t *ix;
-    int r;
-    __device__ __forceinline__ float &D(int e) { return d[e * BM + r]; }
-    __device__ __forceinline__ uint32_t &I(int e) { return ix[e * BM + r]; }
-    __device__ void push(int &n, float v, uint32_t id) {
-        int pos = n++;
-        while (pos > 0) {
-            const int par = (pos - 1) >> 1;
-            if (D(par) >= v) break;
-            D(pos) = D(par);
-            I(pos) = I(par);
-            pos = par;
-        }
-        D(pos) = v;
-        I(pos) = id;
-    }
-    __device__ void sift_down(int n, int pos, float v, uint32_t id) {
-        while (true) {
-            const int l = 2 * pos + 1;
-            if (l >= n) break;
-            const int rr = l + 1;
-            const int m = (rr < n && D(rr) > D(l)) ? rr : l;
-            if (D(m) <= v) break;
-            D(pos) = D(m);
-            I(pos) = I(m);
-            pos = m;
-        }
-        D(pos) = v;
-        I(pos) = id;
-    }
-};
-
 __global__ void __launch_bounds__(kThreads, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap map_qhi, const __grid_constant__ CUtensorMap map_qlo,
              const __grid_constant__ CUtensorMap map_rhi, const __grid_constant__ CUtensorMap map_rlo,
@@ -248,8 +214,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint8_t *sA_lo = base + kATileBytes;
     uint8_t *sB = base + 2 * kATileBytes;  // stage s: hi at s*2*kBTileBytes, lo after it
     float *stash = reinterpret_cast<float *>(base + kStashOff);  // [32 columns][BM rows]
-    float *heap_d = reinterpret_cast<float *>(base + kHeapOff);
-    uint32_t *heap_i = reinterpret_cast<uint32_t *>(base + kHeapOff + (size_t) kMaxTcCandidates * BM * 4);
+    HeapEntry *heaps = reinterpret_cast<HeapEntry *>(base + kHeapOff);  // entry e of row r at e*BM + r
 
     const int nQT = Npad / BM;
     const int nRT = Npad / BN;
@@ -466,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // ---------------- epilogue: warps 2..5 ----------------
         const int quarter = warp & 3;  // TMEM lanes this warp may read
         const int row = quarter * 32 + lane;
-        Heap hp{heap_d, heap_i, row};
+        const Heap4<BM> hp{heaps + row};
         float *my_stash = stash + row;
         int j = 0;
         bool ok = true;
@@ -501,6 +466,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (lane == 0) mbar_arrive(&bar_acc_empty[b]);
                 const int tilebase = rt * BN;
                 const int nvalid = N - tilebase;
+                // the test d2 = nq - 2 acc < thr in accumulator form, acc > (nq - thr) / 2, with
+                // the bound lowered by a margin above both roundings: the masks keep every
+                // column the exact test at the insert keeps (rows past N: none; lists not yet
+                // full: all)
+                float vt;
+                if (!qvalid) {
+                    vt = __int_as_float(0x7f800000);
+                } else if (thr >= FLT_MAX) {
+                    vt = -__int_as_float(0x7f800000);
+                } else {
+                    vt = 0.5f * (nq - thr) - (fabsf(nq) + fabsf(thr)) * 2.384185791015625e-07f;
+                }
                 // kept-candidate masks, built in four independent chains per 32 columns
                 uint32_t mk[2];
 #pragma unroll
@@ -508,10 +485,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                     uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
 #pragma unroll
                     for (int jj = 0; jj < 32; jj += 4) {
-                        q0 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj]), nq) < thr) ? (1u << jj) : 0u;
-                        q1 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj + 1]), nq) < thr) ? (2u << jj) : 0u;
-                        q2 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj + 2]), nq) < thr) ? (4u << jj) : 0u;
-                        q3 |= (fmaf(-2.f, __uint_as_float(v[32 * h + jj + 3]), nq) < thr) ? (8u << jj) : 0u;
+                        q0 |= (__uint_as_float(v[32 * h + jj]) > vt) ? (1u << jj) : 0u;
+                        q1 |= (__uint_as_float(v[32 * h + jj + 1]) > vt) ? (2u << jj) : 0u;
+                        q2 |= (__uint_as_float(v[32 * h + jj + 2]) > vt) ? (4u << jj) : 0u;
+                        q3 |= (__uint_as_float(v[32 * h + jj + 3]) > vt) ? (8u << jj) : 0u;
                     }
                     const int nv = nvalid - 32 * h;
                     const uint32_t lim = nv >= 32 ? 0xffffffffu : (nv <= 0 ? 0u : ((1u << nv) - 1u));
@@ -535,10 +512,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                                 ++nins;
                                 if (n < C) {
                                     hp.push(n, d2, (uint32_t) (colbase + jj));
-                                    if (n == C) thr = hp.D(0);
+                                    if (n == C) thr = hp.top();
                                 } else {
                                     hp.sift_down(n, 0, d2, (uint32_t) (colbase + jj));
-                                    thr = hp.D(0);
+                                    thr = hp.top();
                                 }
                             }
                         }
@@ -551,19 +528,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             if (!ok) break;
             if (qvalid) {
-                // heap sort ascending and write the list
-                for (int end = n - 1; end > 0; --end) {
-                    const float dv = hp.D(end);
-                    const uint32_t iv = hp.I(end);
-                    hp.D(end) = hp.D(0);
-                    hp.I(end) = hp.I(0);
-                    hp.sift_down(end, 0, dv, iv);
-                }
+                hp.sort_ascending(n);
                 // rows and indices back to the caller's numbering
                 const size_t orow = (size_t) (perm ? perm[q] : (uint32_t) q) * C;
                 for (int e = 0; e < C; ++e) {
-                    out_d[orow + e] = e < n ? hp.D(e) : FLT_MAX;
-                    out_i[orow + e] = e < n ? (perm ? perm[hp.I(e)] : hp.I(e)) : 0xffffffffu;
+                    const HeapEntry en = hp.at(e);
+                    out_d[orow + e] = e < n ? en.d : FLT_MAX;
+                    out_i[orow + e] = e < n ? (perm ? perm[en.i] : en.i) : 0xffffffffu;
                 }
             }
         }
