@@ -276,7 +276,7 @@ int Embedding<T>::gradient(double *dC_host, double *sum_Q) {
     p.exag = 1.0;
     p.df = gp_.df;
     if (attr_shape_ < 0) {
-        int tr = tune_attr();
+        int tr = tune_attr(false);
         if (tr) return tr;
     }
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_, p,
@@ -383,7 +383,7 @@ int Embedding<T>::step(const UpdateParams &p, bool) {
     rc = repulsion();
     if (rc) return rc;
     if (attr_shape_ < 0) {
-        rc = tune_attr();
+        rc = tune_attr(true);
         if (rc) return rc;
     }
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], uY_, gains_, nullptr, rep_, N_, D_, p,
@@ -526,11 +526,21 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
 // ---------------------------------------------------------------------------------
 // Graph-captured iteration chunks.  The grid of every iteration is sized on the device
 // (k_geometry) inside a capacity chosen here; the host reads the status once per chunk.
-// Times the attraction pass (gradient only: no state changes) in each launch shape on this
-// embedding's data and keeps the fastest; choices are shared by embeddings of the same size
-// class (type, dimension, log2 N, log2 nnz / N, renumbered or not) within the process.
+//
+// Chooses the attraction pass's launch shape: FITSNE_ATTR_SHAPE fixes it; otherwise, when
+// `measure` is set, the candidate shapes are timed on the attraction pass (gradient only: no
+// state changes) of this embedding's data and the fastest is kept.  Choices are shared by
+// embeddings of the same size class (type, dimension, log2 N, log2 nnz / N, renumbered or not)
+// within the process.  An embedding that will be renumbered for locality (run schedule, N >=
+// kReorderMinN) runs the default shape until its first renumbering and is timed after it, on
+// the numbering of the iterations that follow; one-off gradients (measure false) take the
+// cached choice or the default.
 template <typename T>
-int Embedding<T>::tune_attr() {
+int Embedding<T>::tune_attr(bool measure) {
+    // candidates, the default first: the shapes that came out ahead on some size class
+    // (grad.cu describes them); 16 rows x 2 edges per lane was the fastest at N = 1M
+    static const int kCandidates[] = {3, 0, 2, 9};
+    constexpr int kNumCandidates = (int) (sizeof(kCandidates) / sizeof(kCandidates[0]));
     static std::mutex mu;
     static std::map<std::vector<int>, int> chosen;
     int lgN = 0, lgK = 0;
@@ -538,6 +548,12 @@ int Embedding<T>::tune_attr() {
     const size_t per = N_ ? nnz_ / (size_t) N_ : 0;
     while (((size_t) 1 << (lgK + 1)) <= per) ++lgK;
     const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0};
+    const char *fixed = std::getenv("FITSNE_ATTR_SHAPE");  // a fixed shape index: no tuning, no cache
+    if (fixed && *fixed) {
+        const int sh = std::atoi(fixed);
+        attr_shape_ = (sh >= 0 && sh < kNumAttrShapes) ? sh : 0;
+        return 0;
+    }
     {
         std::lock_guard<std::mutex> lk(mu);
         auto it = chosen.find(key);
@@ -546,13 +562,14 @@ int Embedding<T>::tune_attr() {
             return 0;
         }
     }
+    const bool renumber_ahead = !reordered_ && reorder_enabled_ && N_ >= kReorderMinN;
+    if (!measure || renumber_ahead) {
+        attr_shape_ = kCandidates[0];  // not cached: a later call may measure
+        return 0;
+    }
     const char *e = std::getenv("FITSNE_AUTOTUNE");
-    const char *fixed = std::getenv("FITSNE_ATTR_SHAPE");  // a fixed shape index, no tuning
-    int best = 0;
-    if (fixed && *fixed) {
-        best = std::atoi(fixed);
-        if (best < 0 || best >= kNumAttrShapes) best = 0;
-    } else if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
+    int best = kCandidates[0];
+    if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
         UpdateParams p{};
         p.mode = 0;
         p.exag = 1.0;
@@ -561,7 +578,8 @@ int Embedding<T>::tune_attr() {
         FITSNE_CK(cudaEventCreate(&a));
         FITSNE_CK(cudaEventCreate(&b));
         float best_ms = 0.f;
-        for (int sh = 0; sh < kNumAttrShapes; ++sh) {
+        for (int ci = 0; ci < kNumCandidates; ++ci) {
+            const int sh = kCandidates[ci];
             FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_,
                                             p, red_, st_, sh));
             FITSNE_CK(cudaEventRecord(a, st_));
@@ -572,15 +590,13 @@ int Embedding<T>::tune_attr() {
             FITSNE_CK(cudaEventSynchronize(b));
             float ms = 0.f;
             cudaEventElapsedTime(&ms, a, b);
-            // another shape must beat the default by 3 % (timing noise)
-            if (sh == 0 || ms < 0.97f * best_ms) {
-                if (sh == 0 || ms < best_ms) {
-                    best = sh;
-                    best_ms = ms;
-                }
+            // another shape must beat the best so far by 3 % (timing noise)
+            if (ci == 0 || ms < 0.97f * best_ms) {
+                best = sh;
+                best_ms = ms;
             }
         }
-        launches_ += 4 * kNumAttrShapes;
+        launches_ += 4 * kNumCandidates;
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         if (timing_requested()) {
@@ -601,7 +617,7 @@ int Embedding<T>::tune_attr() {
 template <typename T>
 int Embedding<T>::plan_capacity(int grow) {
     if (attr_shape_ < 0) {
-        int tr = tune_attr();
+        int tr = tune_attr(true);
         if (tr) return tr;
     }
     int nb = nb_last_ > 0 ? nb_last_ : geom_.nb;

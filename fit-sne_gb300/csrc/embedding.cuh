@@ -173,7 +173,7 @@ class Embedding {
     // autotuned launch shape of the attraction pass (-1: not chosen yet); re-chosen after a
     // locality renumbering, since the gathers' locality decides between the shapes
     int attr_shape_ = -1;
-    int tune_attr();
+    int tune_attr(bool measure);
     // graph chunks
     bool graphs_ = true;
     DevGeom *dgeom_ = nullptr;         // device: geometry of the current iteration

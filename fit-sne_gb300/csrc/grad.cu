@@ -553,6 +553,90 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 }
 
 // ---------------------------------------------------------------------------------
+// Row `my` of the attraction kernels: the gradient (exaggeration x attraction amy, minus the
+// repulsion over Z; tsne.cpp:1121-1155) and, in mode 1, the reference's update (gains,
+// momentum, step clipping; tsne.cpp:479-531) into Yout, the new position added to msum; in
+// mode 0 the gradient into dC only.
+template <typename T, int D>
+FITSNE_D void attr_row_update(int my, const T (&amy)[D], const typename YL<T, D>::P (&cmy)[D], const UpdateParams &p,
+                              T zinv, T exag, const T *__restrict__ rep, T *__restrict__ dC, T *__restrict__ gains,
+                              T *__restrict__ uY, T *__restrict__ Yout, typename YL<T, D>::P (&msum)[D]) {
+    typedef typename YL<T, D>::P P;
+    T gr[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) gr[d] = exag * amy[d] - rep[(size_t) my * D + d] * zinv;
+    if (p.mode == 0) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) dC[(size_t) my * D + d] = gr[d];
+        return;
+    }
+    P cn[D];
+    if (p.use_gains) {
+        T u[D];
+        T nrm2 = T(0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            T gn = gains[(size_t) my * D + d];
+            const T uo = uY[(size_t) my * D + d];
+            gn = (sgn(gr[d]) != sgn(uo)) ? (gn + T(0.2)) : (gn * T(0.8));
+            if (gn < T(0.01)) gn = T(0.01);
+            gains[(size_t) my * D + d] = gn;
+            u[d] = T(p.momentum) * uo - T(p.learning_rate) * gn * gr[d];
+            nrm2 += u[d] * u[d];
+        }
+        if (p.max_step_norm > 0) {
+            const T step = sqrt(nrm2);
+            if (step > T(p.max_step_norm)) {
+                const T sc = T(p.max_step_norm) / step;
+#pragma unroll
+                for (int d = 0; d < D; ++d) u[d] *= sc;
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            uY[(size_t) my * D + d] = u[d];
+            cn[d] = padd(cmy[d], u[d]);
+        }
+    } else {
+#pragma unroll
+        for (int d = 0; d < D; ++d) cn[d] = padd(cmy[d], -gr[d]);
+    }
+    YL<T, D>::store(Yout, my, cn);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        if constexpr (sizeof(T) == 4)
+            msum[d] = df_add(msum[d], cn[d]);
+        else
+            msum[d] += cn[d];
+    }
+}
+
+// End of an attraction kernel: the last warp out resets the work counter for the next launch
+// (every warp's last counter increment is ordered before its exit increment by the fence);
+// in mode 1 the grid sum of the new positions gives the mean that the next centring removes.
+template <typename T, int D>
+FITSNE_D void attr_finish(int lane, unsigned int nwarps, int N, const UpdateParams &p, RedScratch r,
+                          const typename YL<T, D>::P (&msum)[D], double *sh) {
+    if (lane == 0) {
+        __threadfence();
+        const unsigned int out = atomicAdd(r.count + 5, 1u);
+        if (out == nwarps - 1) {
+            atomicExch(r.count + 4, 0u);
+            atomicExch(r.count + 5, 0u);
+        }
+    }
+    if (p.mode != 0) {
+        double m[2] = {0.0, 0.0};
+#pragma unroll
+        for (int d = 0; d < D; ++d) m[d] = ptod(msum[d]);
+        if (grid_sum<2>(m, r.part, r.count + 2, sh)) {
+            r.mean[0] = m[0] / (double) N;
+            r.mean[1] = m[1] / (double) N;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
 // CSR attraction fused with the optimiser step (tsne.cpp:1121-1155 and 479-531).
 //
 // Warps take groups of kAttrGroup consecutive rows from a work counter (so that the grid sweeps
@@ -712,74 +796,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__r
             }
         }
         if (!live) continue;
-        // ---- row `my`: gradient and update ----
-        T gr[D];
-#pragma unroll
-        for (int d = 0; d < D; ++d) gr[d] = exag * amy[d] - rep[(size_t) my * D + d] * zinv;
-        if (p.mode == 0) {
-#pragma unroll
-            for (int d = 0; d < D; ++d) dC[(size_t) my * D + d] = gr[d];
-            continue;
-        }
-        P cn[D];
-        if (p.use_gains) {
-            T u[D];
-            T nrm2 = T(0);
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                T gn = gains[(size_t) my * D + d];
-                const T uo = uY[(size_t) my * D + d];
-                gn = (sgn(gr[d]) != sgn(uo)) ? (gn + T(0.2)) : (gn * T(0.8));
-                if (gn < T(0.01)) gn = T(0.01);
-                gains[(size_t) my * D + d] = gn;
-                u[d] = T(p.momentum) * uo - T(p.learning_rate) * gn * gr[d];
-                nrm2 += u[d] * u[d];
-            }
-            if (p.max_step_norm > 0) {
-                const T step = sqrt(nrm2);
-                if (step > T(p.max_step_norm)) {
-                    const T sc = T(p.max_step_norm) / step;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) u[d] *= sc;
-                }
-            }
-#pragma unroll
-            for (int d = 0; d < D; ++d) {
-                uY[(size_t) my * D + d] = u[d];
-                cn[d] = padd(cmy[d], u[d]);
-            }
-        } else {
-#pragma unroll
-            for (int d = 0; d < D; ++d) cn[d] = padd(cmy[d], -gr[d]);
-        }
-        YL<T, D>::store(Yout, my, cn);
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            if constexpr (sizeof(T) == 4)
-                msum[d] = df_add(msum[d], cn[d]);
-            else
-                msum[d] += cn[d];
-        }
+        attr_row_update<T, D>(my, amy, cmy, p, zinv, exag, rep, dC, gains, uY, Yout, msum);
     }
-    // the last warp out resets the work counter for the next launch (every warp's last
-    // counter increment is ordered before its exit increment by the fence)
-    if (lane == 0) {
-        __threadfence();
-        const unsigned int out = atomicAdd(r.count + 5, 1u);
-        if (out == nwarps - 1) {
-            atomicExch(r.count + 4, 0u);
-            atomicExch(r.count + 5, 0u);
-        }
-    }
-    if (p.mode != 0) {
-        double m[2] = {0.0, 0.0};
-#pragma unroll
-        for (int d = 0; d < D; ++d) m[d] = ptod(msum[d]);
-        if (grid_sum<2>(m, r.part, r.count + 2, sh)) {
-            r.mean[0] = m[0] / (double) N;
-            r.mean[1] = m[1] / (double) N;
-        }
-    }
+    attr_finish<T, D>(lane, nwarps, N, p, r, msum, sh);
 }
 
 // ---------------------------------------------------------------------------------

@@ -102,3 +102,46 @@ def test_fp32_box_index_agrees_with_fp64_on_a_box_edge(gpu_lib, golden):
     g32, g64 = out[32][0], out[64][0]
     assert np.linalg.norm(g32[i] - g64[i]) / np.linalg.norm(g64[i]) < 1e-4
     assert rel_l2(g32, g64) < 1e-5
+
+
+N_SHAPES = 10  # attraction launch shapes (kNumAttrShapes)
+
+
+@pytest.mark.parametrize("shape", range(N_SHAPES))
+@pytest.mark.parametrize("bits", [32, 64])
+@pytest.mark.parametrize("name,yk", [("g2_df1", "Y2"), ("g1_df1", "Y1")])
+def test_every_attraction_shape_gives_the_reference_gradient(gpu_lib, golden, monkeypatch, bits, shape, name, yk):
+    """Each launch shape of the attraction pass (the autotuner's candidates, fixed through
+    FITSNE_ATTR_SHAPE) computes the reference's gradient within the FP32 / FP64 tolerances."""
+    monkeypatch.setenv("FITSNE_ATTR_SHAPE", str(shape))
+    row, col, val = _P(golden)
+    gpu_lib.set_precision(bits)
+    try:
+        dC, z = gpu_lib.fft_gradient(row, col, val, golden[yk], 3, 1.0, 50, 1.0)
+    finally:
+        gpu_lib.set_precision(32)
+    assert rel_l2(dC, golden[name + "_dC"]) < TOL[bits][0]
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_every_attraction_shape_takes_the_same_steps(gpu_lib, monkeypatch, bits):
+    """The fused update (gains, momentum, clipping, double-float Y) is the same code in every
+    shape: 3 iterations from the same start agree with shape 0's up to the summation order of
+    the attraction (FP32 1e-4, FP64 1e-9 relative).  Longer runs drift apart in FP32: the
+    gains rule jumps (+0.2 or x0.8) on the sign of a gradient component, and a component near
+    zero flips with the last bits of the sum (20 iterations: 6e-4 between shapes 0 and 1)."""
+    rng = np.random.default_rng(4)
+    c = rng.standard_normal((6, 10)) * 4.0
+    X = c[rng.integers(0, 6, 3000)] + rng.standard_normal((3000, 10))
+    Y0 = rng.standard_normal((3000, 2)) * 1e-4
+    gpu_lib.set_precision(bits)
+    try:
+        out = []
+        for shape in range(N_SHAPES):
+            monkeypatch.setenv("FITSNE_ATTR_SHAPE", str(shape))
+            Y, _ = gpu_lib.run(X, Y0=Y0, perplexity=30.0, max_iter=3, learning_rate=250.0)
+            out.append(Y)
+    finally:
+        gpu_lib.set_precision(32)
+    for shape in range(1, N_SHAPES):
+        assert rel_l2(out[shape], out[0]) < (1e-4 if bits == 32 else 1e-9), shape
