@@ -1,5 +1,6 @@
 // Host driver of the per-iteration kernels (see embedding.cuh).
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <mutex>
 #include <map>
@@ -35,6 +36,7 @@ Embedding<T>::~Embedding() {
     cudaFree(val_);
     cudaFree(Y_[0]);
     cudaFree(Y_[1]);
+    cudaFree(yh_);
     cudaFree(uY_);
     cudaFree(gains_);
     cudaFree(rep_);
@@ -88,6 +90,10 @@ int Embedding<T>::alloc_common(int N, int D, size_t nnz) {
     FITSNE_CK(cudaMalloc(&val_, sizeof(T) * (nnz ? nnz : 1)));
     FITSNE_CK(cudaMalloc(&Y_[0], sizeof(T) * (size_t) N * W));
     FITSNE_CK(cudaMalloc(&Y_[1], sizeof(T) * (size_t) N * W));
+    if (sizeof(T) == 4) {  // FP32 form: the neighbour positions the attraction gathers (k_gather writes them)
+        FITSNE_CK(cudaMalloc(&yh_, sizeof(float) * (size_t) N * D));
+        FITSNE_CK(cudaMemsetAsync(yh_, 0, sizeof(float) * (size_t) N * D, st_));
+    }
     FITSNE_CK(cudaMalloc(&uY_, sizeof(T) * (size_t) N * D));
     FITSNE_CK(cudaMalloc(&gains_, sizeof(T) * (size_t) N * D));
     FITSNE_CK(cudaMalloc(&rep_, sizeof(T) * (size_t) N * D));
@@ -256,7 +262,7 @@ int Embedding<T>::repulsion() {
     else
         FITSNE_CK(conv1d_launch<T>(grid_in_, grid_out_, M, plan_, tw_[L_], work_a_, geom_.hk, gp_.df, mode, st_));
     if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][3], st_));
-    FITSNE_CK(launch_gather<T>(Y_[cur_], N_, D_, geom_, grid_out_, mode, rep_, red_, st_));
+    FITSNE_CK(launch_gather<T>(Y_[cur_], N_, D_, geom_, grid_out_, mode, rep_, red_, st_, yh_));
     if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][4], st_));
     launches_ += 1 + (D_ == 2 ? 5 : 2) + 1;  // spread, convolution passes, gather
     return 0;
@@ -280,7 +286,7 @@ int Embedding<T>::gradient(double *dC_host, double *sum_Q) {
         if (tr) return tr;
     }
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_, p,
-                                    red_, st_, attr_shape_));
+                                    red_, st_, attr_shape_, yh_));
     launches_ += 2;
     std::vector<T> tmp((size_t) N_ * D_);
     FITSNE_CK(cudaMemcpyAsync(tmp.data(), dC_, sizeof(T) * tmp.size(), cudaMemcpyDeviceToHost, st_));
@@ -387,7 +393,7 @@ int Embedding<T>::step(const UpdateParams &p, bool) {
         if (rc) return rc;
     }
     FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], uY_, gains_, nullptr, rep_, N_, D_, p,
-                                    red_, st_, attr_shape_));
+                                    red_, st_, attr_shape_, yh_));
     launches_ += 2;  // centre + attraction
     if (timing_) {
         FITSNE_CK(cudaEventRecord(evs_[tb_][5], st_));
@@ -581,11 +587,11 @@ int Embedding<T>::tune_attr(bool measure) {
         for (int ci = 0; ci < kNumCandidates; ++ci) {
             const int sh = kCandidates[ci];
             FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_,
-                                            p, red_, st_, sh));
+                                            p, red_, st_, sh, yh_));
             FITSNE_CK(cudaEventRecord(a, st_));
             for (int r = 0; r < 3; ++r)
                 FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_,
-                                                D_, p, red_, st_, sh));
+                                                D_, p, red_, st_, sh, yh_));
             FITSNE_CK(cudaEventRecord(b, st_));
             FITSNE_CK(cudaEventSynchronize(b));
             float ms = 0.f;
@@ -689,9 +695,9 @@ int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_f
                                            gp_.df, mode, st_));
         else
             FITSNE_CK(conv1d_launch_dev<T>(grid_in_, grid_out_, L_cap_, cg, tw_dev_, work_a_, gp_.df, mode, st_));
-        FITSNE_CK(launch_gather_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_out_, mode, rep_, red_, st_));
+        FITSNE_CK(launch_gather_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_out_, mode, rep_, red_, st_, yh_));
         FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[c], Y_[1 - c], uY_, gains_, nullptr, rep_, N_, D_, p,
-                                        red_, st_, attr_shape_ < 0 ? 0 : attr_shape_));
+                                        red_, st_, attr_shape_ < 0 ? 0 : attr_shape_, yh_));
         c = 1 - c;
     }
     FITSNE_CK(cudaMemcpyAsync(h_gstat_, gstatus_, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -845,10 +851,16 @@ int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, doubl
         return 0;
     };
     const unsigned long long l0 = launches_;
+    // host time by phase (reported under FITSNE_TIMING)
+    using clk = std::chrono::steady_clock;
+    double t_first = 0, t_reorder = 0, t_launch = 0, t_wait = 0, t_after = 0;
+    auto since = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    const unsigned long long cap0 = captures_, upd0 = updates_;
     FITSNE_CK(cudaEventRecord(evr_[0], st_));
     int it = it0;
     if (it < it1) {
         // first iteration on the host path: it sizes the grid and fixes the launch shapes
+        const auto t = clk::now();
         if (reorder_due(it)) {
             int rr = reorder();
             if (rr) return rr;
@@ -859,11 +871,16 @@ int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, doubl
         rc = after(it);
         if (rc) return rc;
         ++it;
+        FITSNE_CK(cudaStreamSynchronize(st_));
+        t_first += since(t);
     }
     while (it < it1) {
         if (reorder_due(it)) {
+            const auto t = clk::now();
             int rr = reorder();
             if (rr) return rr;
+            FITSNE_CK(cudaStreamSynchronize(st_));
+            t_reorder += since(t);
         }
         // chunks of at most kMaxChunk iterations, so that the grid capacity follows the
         // embedding's growth and a repeated chunk costs little
@@ -876,24 +893,36 @@ int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, doubl
         const UpdateParams p = params(it);
         int grow = 0;
         while (true) {
+            auto t = clk::now();
             int rc = launch_chunk(p, len, grow);
             if (rc) return rc;
+            t_launch += since(t);
+            t = clk::now();
             FITSNE_CK(cudaStreamSynchronize(st_));
+            t_wait += since(t);
             rc = finish_chunk(len);
             if (rc < 0) return rc;
             if (rc == 0) break;
             grow = 1;  // the embedding outgrew the capacity inside the chunk: larger grid, same chunk
         }
+        const auto t = clk::now();
         for (int k = it; k < end; ++k) {
             int rc = after(k);
             if (rc) return rc;
         }
+        t_after += since(t);
         it = end;
     }
     FITSNE_CK(cudaEventRecord(evr_[1], st_));
     FITSNE_CK(cudaEventSynchronize(evr_[1]));
     cudaEventElapsedTime(&times_.run_ms, evr_[0], evr_[1]);
     times_.launches = launches_ - l0;
+    if (timing_requested())
+        std::fprintf(stderr,
+                     "[fitsne] iterations %d-%d: first (host path, tuning) %.3f s, renumbering %.3f s, chunk "
+                     "capture/update/launch %.3f s (%llu captures, %llu updates), chunk execution wait %.3f s, "
+                     "KL and switches %.3f s\n",
+                     it0, it1, t_first, t_reorder, t_launch, captures_ - cap0, updates_ - upd0, t_wait, t_after);
     return 0;
 }
 

@@ -140,6 +140,7 @@ class Embedding {
     uint32_t *row_ = nullptr, *col_ = nullptr;
     T *val_ = nullptr;
     T *Y_[2] = {nullptr, nullptr};
+    float *yh_ = nullptr;  // FP32 form: high words of Y_[cur_] (written by the gather pass)
     int cur_ = 0;
     bool mean_pending_ = false;
     T *uY_ = nullptr, *gains_ = nullptr, *rep_ = nullptr, *dC_ = nullptr;

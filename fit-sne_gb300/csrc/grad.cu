@@ -497,7 +497,7 @@ template <typename T, int D, int NT>
 __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int N, BoxP<T> b,
                                                    const Cell4<T> *__restrict__ pot, int mode,
                                                    T *__restrict__ rep, RedScratch r,
-                                                   const DevGeom *__restrict__ dg) {
+                                                   const DevGeom *__restrict__ dg, float *__restrict__ yh) {
     typedef typename YL<T, D>::P P;
     if (dg) b = make_box(dg->g, (T *) nullptr);
     __shared__ double sh[32];
@@ -506,6 +506,15 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         P c[D];
         YL<T, D>::load(Y, i, c);
+        if constexpr (sizeof(T) == 4) {
+            // the FP32 positions (high words) that the attraction gathers as neighbours
+            if (yh) {
+                if constexpr (D == 2)
+                    reinterpret_cast<float2 *>(yh)[i] = make_float2(c[0].hi, c[1].hi);
+                else
+                    yh[i] = c[0].hi;
+            }
+        }
         int bx[D];
         T t[D];
         T w[D][NT > 0 ? NT : kMaxInterp];
@@ -653,7 +662,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__r
                                                  const T *__restrict__ val, const T *__restrict__ Yin,
                                                  T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
                                                  T *__restrict__ dC, const T *__restrict__ rep, int N,
-                                                 UpdateParams p, RedScratch r) {
+                                                 UpdateParams p, RedScratch r, const float *__restrict__ yh) {
     typedef typename YL<T, D>::P P;
     __shared__ double sh[2 * 32];
     const unsigned full = 0xffffffffu;
@@ -773,7 +782,21 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__r
                 }
                 P cj[kAttrUnroll][D];
 #pragma unroll
-                for (int u = 0; u < kAttrUnroll; ++u) YL<T, D>::load(Yin, (int) j[u], cj[u]);
+                for (int u = 0; u < kAttrUnroll; ++u) {
+                    if constexpr (sizeof(T) == 4) {
+                        if (yh) {  // FP32 neighbour positions (high words only): 8 instead of 16 bytes
+                            if constexpr (D == 2) {
+                                const float2 h = __ldg(reinterpret_cast<const float2 *>(yh) + j[u]);
+                                cj[u][0] = {h.x, 0.f};
+                                cj[u][1] = {h.y, 0.f};
+                            } else {
+                                cj[u][0] = {__ldg(yh + j[u]), 0.f};
+                            }
+                            continue;
+                        }
+                    }
+                    YL<T, D>::load(Yin, (int) j[u], cj[u]);
+                }
 #pragma unroll
                 for (int u = 0; u < kAttrUnroll; ++u) {
                     T dx[D];
@@ -931,34 +954,34 @@ cudaError_t launch_spread_dev(const T *Y, int N, int D, int nterms, const DevGeo
 
 template <typename T>
 cudaError_t gather_impl(const T *Y, int N, int D, int nterms, const BoxP<T> &b, const Cell4<T> *pot, int mode, T *rep,
-                        RedScratch r, const DevGeom *dg, cudaStream_t st) {
+                        RedScratch r, const DevGeom *dg, float *yh, cudaStream_t st) {
     const int g = grid_for(N, kBlock, kRedGrid);
     if (D == 2) {
         if (nterms == 3)
-            k_gather<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
+            k_gather<T, 2, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg, yh);
         else
-            k_gather<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
+            k_gather<T, 2, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg, yh);
     } else {
         if (nterms == 3)
-            k_gather<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
+            k_gather<T, 1, 3><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg, yh);
         else
-            k_gather<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg);
+            k_gather<T, 1, 0><<<g, kBlock, 0, st>>>(Y, N, b, pot, mode, rep, r, dg, yh);
     }
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &gg, const Cell4<T> *pot, int mode, T *rep,
-                          RedScratch r, cudaStream_t st) {
-    return gather_impl<T>(Y, N, D, gg.nterms, make_box(gg, (T *) nullptr), pot, mode, rep, r, nullptr, st);
+                          RedScratch r, cudaStream_t st, float *yh) {
+    return gather_impl<T>(Y, N, D, gg.nterms, make_box(gg, (T *) nullptr), pot, mode, rep, r, nullptr, yh, st);
 }
 
 template <typename T>
 cudaError_t launch_gather_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, const Cell4<T> *pot, int mode,
-                              T *rep, RedScratch r, cudaStream_t st) {
+                              T *rep, RedScratch r, cudaStream_t st, float *yh) {
     BoxP<T> b{};
     b.nterms = nterms;
-    return gather_impl<T>(Y, N, D, nterms, b, pot, mode, rep, r, dg, st);
+    return gather_impl<T>(Y, N, D, nterms, b, pot, mode, rep, r, dg, yh, st);
 }
 
 namespace {
@@ -1003,7 +1026,8 @@ cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min
 
 template <typename T, int D, int G, int U, bool B = false, bool PP = false, int MB = 1>
 cudaError_t attr_launch(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout, T *uY,
-                        T *gains, T *dC, const T *rep, int N, const UpdateParams &p, RedScratch r, cudaStream_t st) {
+                        T *gains, T *dC, const T *rep, int N, const UpdateParams &p, RedScratch r, cudaStream_t st,
+                        const float *yh) {
     // one resident wave: the warps take row groups from a counter
     static int wave = 0;
     if (wave == 0) {
@@ -1016,39 +1040,39 @@ cudaError_t attr_launch(const uint32_t *row, const uint32_t *col, const T *val, 
         wave = std::min(kMaxRedBlocks, nsm * (per_sm > 0 ? per_sm : 1));
     }
     const int g = grid_for(((long long) N + 31) / 32 * 32, kBlock, wave);
-    k_attr<T, D, G, U, B, PP, MB><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r);
+    k_attr<T, D, G, U, B, PP, MB><<<g, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, yh);
     return cudaGetLastError();
 }
 
 template <typename T, int D>
 cudaError_t attr_dispatch(int shape, const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
                           T *uY, T *gains, T *dC, const T *rep, int N, const UpdateParams &p, RedScratch r,
-                          cudaStream_t st) {
+                          cudaStream_t st, const float *yh) {
     switch (shape) {
-        case 1: return attr_launch<T, D, 32, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
-        case 2: return attr_launch<T, D, 8, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
-        case 3: return attr_launch<T, D, 16, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
-        case 4: return attr_launch<T, D, 32, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
-        case 5: return attr_launch<T, D, 16, 4, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+        case 1: return attr_launch<T, D, 32, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
+        case 2: return attr_launch<T, D, 8, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
+        case 3: return attr_launch<T, D, 16, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
+        case 4: return attr_launch<T, D, 32, 2>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
+        case 5: return attr_launch<T, D, 16, 4, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
         case 6:
-            return attr_launch<T, D, 16, 4, false, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+            return attr_launch<T, D, 16, 4, false, true>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
         case 7:
             return attr_launch<T, D, 16, 4, false, false, 6>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r,
-                                                            st);
+                                                            st, yh);
         case 8:
             return attr_launch<T, D, 8, 4, false, false, 6>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r,
-                                                           st);
-        case 9: return attr_launch<T, D, 16, 5>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
-        default: return attr_launch<T, D, 16, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+                                                           st, yh);
+        case 9: return attr_launch<T, D, 16, 5>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
+        default: return attr_launch<T, D, 16, 4>(row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
     }
 }
 
 template <typename T>
 cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
                                T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
-                               RedScratch r, cudaStream_t st, int shape) {
-    if (D == 2) return attr_dispatch<T, 2>(shape, row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
-    return attr_dispatch<T, 1>(shape, row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st);
+                               RedScratch r, cudaStream_t st, int shape, const float *yh) {
+    if (D == 2) return attr_dispatch<T, 2>(shape, row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
+    return attr_dispatch<T, 1>(shape, row, col, val, Yin, Yout, uY, gains, dC, rep, N, p, r, st, yh);
 }
 
 int attr_shape_info(int shape, int *group, int *unroll) {
@@ -1100,14 +1124,14 @@ cudaError_t launch_cast_from_double(const double *src, T *dst, size_t n, cudaStr
     template cudaError_t launch_center_minmax<T>(T *, int, int, int, int, RedScratch, cudaStream_t);                \
     template cudaError_t launch_spread<T>(const T *, int, int, const GridGeom &, Cell4<T> *, cudaStream_t);     \
     template cudaError_t launch_gather<T>(const T *, int, int, const GridGeom &, const Cell4<T> *, int, T *,     \
-                                          RedScratch, cudaStream_t);                                            \
+                                          RedScratch, cudaStream_t, float *);                                   \
     template cudaError_t launch_gather_dev<T>(const T *, int, int, int, const DevGeom *, const Cell4<T> *, int,  \
-                                              T *, RedScratch, cudaStream_t);                                   \
+                                              T *, RedScratch, cudaStream_t, float *);                          \
     template cudaError_t launch_spread_dev<T>(const T *, int, int, int, const DevGeom *, Cell4<T> *,            \
                                               cudaStream_t);                                                    \
     template cudaError_t launch_attr_update<T>(const uint32_t *, const uint32_t *, const T *, const T *, T *,    \
                                                T *, T *, T *, const T *, int, int, const UpdateParams &,         \
-                                               RedScratch, cudaStream_t, int);                                  \
+                                               RedScratch, cudaStream_t, int, const float *);                   \
     template cudaError_t launch_kl<T>(const uint32_t *, const uint32_t *, const T *, const T *, int, int, double, \
                                       double, RedScratch, cudaStream_t);                                        \
     template cudaError_t launch_y_from_double<T>(const double *, T *, int, int, cudaStream_t);                  \

@@ -131,16 +131,17 @@ template <typename T>
 cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, int excl, RedScratch r, cudaStream_t st);
 template <typename T>
 cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &g, Cell4<T> *grid, cudaStream_t st);
+// yh (may be null): FP32 form only, receives the high words of the positions (D floats per point)
 template <typename T>
 cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &g, const Cell4<T> *pot, int mode, T *rep,
-                          RedScratch r, cudaStream_t st);
+                          RedScratch r, cudaStream_t st, float *yh = nullptr);
 // As launch_spread / launch_gather with the geometry read from device memory.
 template <typename T>
 cudaError_t launch_spread_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, Cell4<T> *grid,
                               cudaStream_t st);
 template <typename T>
 cudaError_t launch_gather_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, const Cell4<T> *pot, int mode,
-                              T *rep, RedScratch r, cudaStream_t st);
+                              T *rep, RedScratch r, cudaStream_t st, float *yh = nullptr);
 // Grid of the current iteration from r.mnmx into dg (see k_geometry in grad.cu).
 cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min_num, int nb_cap, int L_cap,
                             DevGeom *dg, int *status_acc, cudaStream_t st);
@@ -148,10 +149,13 @@ cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min
 // the shape of an index.
 constexpr int kNumAttrShapes = 10;
 int attr_shape_info(int shape, int *group, int *unroll);
+// yh (FP32 form only, may be null): the FP32 positions k_gather wrote for this Y, which the
+// attraction then gathers as its neighbours' positions (8 instead of 16 bytes per point in
+// 2-D; the neighbour's low word, at most 2^-24 |y| / 2, is dropped from y_i - y_j).
 template <typename T>
 cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
                                T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
-                               RedScratch r, cudaStream_t st, int shape = 0);
+                               RedScratch r, cudaStream_t st, int shape = 0, const float *yh = nullptr);
 template <typename T>
 cudaError_t launch_kl(const uint32_t *row, const uint32_t *col, const T *val, const T *Y, int N, int D, double exag,
                       double df, RedScratch r, cudaStream_t st);

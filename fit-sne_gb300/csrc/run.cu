@@ -140,11 +140,24 @@ int build_P(const double *X, int N, int D, double perplexity, int K, double sigm
 template <typename T>
 int optimise(const DevCSR &P, double *Y, int N, int no_dims, const GridParams &gp, const Schedule &s, double *costs,
              cudaStream_t st, bool vb) {
+    const auto t0 = std::chrono::steady_clock::now();
     Embedding<T> emb;
     int rc = emb.init_device(N, no_dims, P.row, P.col, P.val, P.nnz, Y, gp, st);
+    const auto t1 = std::chrono::steady_clock::now();
     if (!rc) rc = emb.run_schedule(s, 0, s.max_iter, costs, vb);
+    const auto t2 = std::chrono::steady_clock::now();
     if (!rc) rc = emb.get_Y(Y);
     if (rc) return set_error(rc == -13 ? FITSNE_E_GRID : FITSNE_E_CUDA, emb.error());
+    if (timing_requested()) {
+        auto sec = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+            return std::chrono::duration<double>(b - a).count();
+        };
+        std::fprintf(stderr,
+                     "[fitsne] embedding: set-up %.3f s, %d iterations %.3f s (%zu kernel launches, %d graph "
+                     "captures), result %.3f s\n",
+                     sec(t0, t1), s.max_iter, sec(t1, t2), (size_t) emb.last_times().launches, (int) emb.graph_captures(),
+                     sec(t2, std::chrono::steady_clock::now()));
+    }
     return 0;
 }
 
@@ -281,6 +294,7 @@ int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexit
     if (!(df > 0)) return set_error(FITSNE_E_ARG, "df must be positive");
     if (perplexity == 0 && (perplexity_list_length < 1 || !perplexity_list))
         return set_error(FITSNE_E_ARG, "perplexity 0 needs a perplexity list");
+    const auto tstart = std::chrono::steady_clock::now();
     int rc = check_cuda_device();
     if (rc) return rc;
     if (max_iter < 0) max_iter = 0;
@@ -331,6 +345,9 @@ int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexit
     if (vb)
         std::printf("Input similarities computed (nnz = %zu); learning embedding (FP%d form)...\n", P.nnz,
                     precision_bits());
+    if (timing_requested())
+        std::fprintf(stderr, "[fitsne] device check + input similarities: %.3f s\n",
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - tstart).count());
     GridParams gp;
     gp.nterms = nterms;
     gp.intervals_per_integer = intervals_per_integer;
