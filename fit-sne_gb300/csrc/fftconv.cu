@@ -204,21 +204,13 @@ FITSNE_D void unpack_r2c(const C *Zs, int L, int kb, C &F, C &G) {
 }
 
 template <typename T>
-__global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
-                              typename Cx<T>::t *__restrict__ krow, T h, T df, int mode,
-                              const ConvGeom *__restrict__ cg) {
+FITSNE_D void kernel_rows_body(int r, int M, const FftPlan &pl, const typename Cx<T>::t *__restrict__ tw,
+                               typename Cx<T>::t *__restrict__ krow, T h, T df, int mode) {
     typedef typename Cx<T>::t C;
-    if (cg) {
-        M = cg->M;
-        pl = cg->plan;
-        h = (T) cg->h;
-        if ((int) blockIdx.x >= 2 * M - 1) return;
-    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *bufa = reinterpret_cast<C *>(smem_raw);
     C *bufb = bufa + 2 * L;
-    const int r = blockIdx.x;
     const int a = (r < M) ? r : (L - (2 * M - 1 - r));
     const int dx = (a < M) ? a : a - L;
     for (int b = threadIdx.x; b < L; b += blockDim.x) {
@@ -244,20 +236,26 @@ __global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__rest
 }
 
 template <typename T>
-__global__ void k_kernel_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
-                              const typename Cx<T>::t *__restrict__ krow, KSpec<T> *__restrict__ kspec,
+__global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
+                              typename Cx<T>::t *__restrict__ krow, T h, T df, int mode,
                               const ConvGeom *__restrict__ cg) {
-    typedef typename Cx<T>::t C;
     if (cg) {
         M = cg->M;
         pl = cg->plan;
-        if ((int) blockIdx.x >= pl.L / 2 + 1) return;
+        h = (T) cg->h;
+        if ((int) blockIdx.x >= 2 * M - 1) return;
     }
+    kernel_rows_body<T>(blockIdx.x, M, pl, tw, krow, h, df, mode);
+}
+
+template <typename T>
+FITSNE_D void kernel_cols_body(int kb, int M, const FftPlan &pl, const typename Cx<T>::t *__restrict__ tw,
+                               const typename Cx<T>::t *__restrict__ krow, KSpec<T> *__restrict__ kspec) {
+    typedef typename Cx<T>::t C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *spec = reinterpret_cast<C *>(smem_raw);
     C *scratch = spec + 4 * L;
-    const int kb = blockIdx.x;
     for (int f = 0; f < 4; ++f)
         for (int a = threadIdx.x; a < L; a += blockDim.x) {
             const bool valid = (a < M) || (a > L - M);
@@ -283,20 +281,25 @@ __global__ void k_kernel_cols(int M, FftPlan pl, const typename Cx<T>::t *__rest
 }
 
 template <typename T>
-__global__ void k_data_rows(const Cell4<T> *__restrict__ grid, int M, FftPlan pl,
-                            const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ d1,
-                            const ConvGeom *__restrict__ cg) {
-    typedef typename Cx<T>::t C;
+__global__ void k_kernel_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
+                              const typename Cx<T>::t *__restrict__ krow, KSpec<T> *__restrict__ kspec,
+                              const ConvGeom *__restrict__ cg) {
     if (cg) {
         M = cg->M;
         pl = cg->plan;
-        if ((int) blockIdx.x >= M) return;
+        if ((int) blockIdx.x >= pl.L / 2 + 1) return;
     }
+    kernel_cols_body<T>(blockIdx.x, M, pl, tw, krow, kspec);
+}
+
+template <typename T>
+FITSNE_D void data_rows_body(int a, const Cell4<T> *__restrict__ grid, int M, const FftPlan &pl,
+                             const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ d1) {
+    typedef typename Cx<T>::t C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *bufa = reinterpret_cast<C *>(smem_raw);
     C *bufb = bufa + 2 * L;
-    const int a = blockIdx.x;
     for (int b = threadIdx.x; b < L; b += blockDim.x) {
         Cell4<T> v;
         if (b < M)
@@ -320,20 +323,26 @@ __global__ void k_data_rows(const Cell4<T> *__restrict__ grid, int M, FftPlan pl
 }
 
 template <typename T>
-__global__ void k_data_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
-                            const typename Cx<T>::t *__restrict__ d1, const KSpec<T> *__restrict__ kspec,
-                            typename Cx<T>::t *__restrict__ d2, int mode, const ConvGeom *__restrict__ cg) {
-    typedef typename Cx<T>::t C;
+__global__ void k_data_rows(const Cell4<T> *__restrict__ grid, int M, FftPlan pl,
+                            const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ d1,
+                            const ConvGeom *__restrict__ cg) {
     if (cg) {
         M = cg->M;
         pl = cg->plan;
-        if ((int) blockIdx.x >= pl.L / 2 + 1) return;
+        if ((int) blockIdx.x >= M) return;
     }
+    data_rows_body<T>(blockIdx.x, grid, M, pl, tw, d1);
+}
+
+template <typename T>
+FITSNE_D void data_cols_body(int kb, int M, const FftPlan &pl, const typename Cx<T>::t *__restrict__ tw,
+                             const typename Cx<T>::t *__restrict__ d1, const KSpec<T> *__restrict__ kspec,
+                             typename Cx<T>::t *__restrict__ d2, int mode) {
+    typedef typename Cx<T>::t C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *spec = reinterpret_cast<C *>(smem_raw);
     C *scratch = spec + 4 * L;
-    const int kb = blockIdx.x;
     for (int f = 0; f < 4; ++f)
         for (int a = threadIdx.x; a < L; a += blockDim.x)
             spec[f * L + a] = (a < M) ? d1[((size_t) f * M + a) * H + kb] : mkc(T(0), T(0));
@@ -377,20 +386,25 @@ __global__ void k_data_cols(int M, FftPlan pl, const typename Cx<T>::t *__restri
 }
 
 template <typename T>
-__global__ void k_data_rows_inv(const typename Cx<T>::t *__restrict__ d2, int M, FftPlan pl,
-                                const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out,
-                                const ConvGeom *__restrict__ cg) {
-    typedef typename Cx<T>::t C;
+__global__ void k_data_cols(int M, FftPlan pl, const typename Cx<T>::t *__restrict__ tw,
+                            const typename Cx<T>::t *__restrict__ d1, const KSpec<T> *__restrict__ kspec,
+                            typename Cx<T>::t *__restrict__ d2, int mode, const ConvGeom *__restrict__ cg) {
     if (cg) {
         M = cg->M;
         pl = cg->plan;
-        if ((int) blockIdx.x >= M) return;
+        if ((int) blockIdx.x >= pl.L / 2 + 1) return;
     }
+    data_cols_body<T>(blockIdx.x, M, pl, tw, d1, kspec, d2, mode);
+}
+
+template <typename T>
+FITSNE_D void data_rows_inv_body(int a, const typename Cx<T>::t *__restrict__ d2, int M, const FftPlan &pl,
+                                 const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out) {
+    typedef typename Cx<T>::t C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
     C *bufa = reinterpret_cast<C *>(smem_raw);
     C *bufb = bufa + 2 * L;
-    const int a = blockIdx.x;
     for (int kb = threadIdx.x; kb < L; kb += blockDim.x) {
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -421,6 +435,18 @@ __global__ void k_data_rows_inv(const typename Cx<T>::t *__restrict__ d2, int M,
         v.d = res[L + b].y;
         out[(size_t) a * M + b] = v;
     }
+}
+
+template <typename T>
+__global__ void k_data_rows_inv(const typename Cx<T>::t *__restrict__ d2, int M, FftPlan pl,
+                                const typename Cx<T>::t *__restrict__ tw, Cell4<T> *__restrict__ out,
+                                const ConvGeom *__restrict__ cg) {
+    if (cg) {
+        M = cg->M;
+        pl = cg->plan;
+        if ((int) blockIdx.x >= M) return;
+    }
+    data_rows_inv_body<T>(blockIdx.x, d2, M, pl, tw, out);
 }
 
 // ---- 1-D ----
@@ -604,6 +630,121 @@ cudaError_t twiddles_dev(const ConvGeom *cg, typename Cx<T>::t *tw, cudaStream_t
     k_twiddles_geom<T><<<8, 256, 0, st>>>(cg, tw);
     return cudaGetLastError();
 }
+
+// ---- batched 2-D convolution: one launch per pass for all jobs ----
+namespace {
+template <typename T>
+__global__ void k_bkernel_rows(FftBatchMap m, const FftBatchJob *__restrict__ jobs,
+                               const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ work_a, T df,
+                               int mode) {
+    const int j = m.job[blockIdx.x];
+    const FftBatchJob jb = jobs[j];
+    const int M = jb.cg->M;
+    const FftPlan pl = jb.cg->plan;
+    const int r = (int) blockIdx.x - m.first[j];
+    if (r >= 2 * M - 1) return;
+    kernel_rows_body<T>(r, M, pl, tw + jb.tw0, work_a + jb.work0, (T) jb.cg->h, df, mode);
+}
+
+template <typename T>
+__global__ void k_bkernel_cols(FftBatchMap m, const FftBatchJob *__restrict__ jobs,
+                               const typename Cx<T>::t *__restrict__ tw, const typename Cx<T>::t *__restrict__ work_a,
+                               KSpec<T> *__restrict__ kspec) {
+    const int j = m.job[blockIdx.x];
+    const FftBatchJob jb = jobs[j];
+    const int M = jb.cg->M;
+    const FftPlan pl = jb.cg->plan;
+    const int kb = (int) blockIdx.x - m.first[j];
+    if (kb >= pl.L / 2 + 1) return;
+    kernel_cols_body<T>(kb, M, pl, tw + jb.tw0, work_a + jb.work0, kspec + jb.kspec0);
+}
+
+template <typename T>
+__global__ void k_bdata_rows(FftBatchMap m, const FftBatchJob *__restrict__ jobs, const Cell4<T> *__restrict__ grid,
+                             const typename Cx<T>::t *__restrict__ tw, typename Cx<T>::t *__restrict__ work_b) {
+    const int j = m.job[blockIdx.x];
+    const FftBatchJob jb = jobs[j];
+    const int M = jb.cg->M;
+    const FftPlan pl = jb.cg->plan;
+    const int a = (int) blockIdx.x - m.first[j];
+    if (a >= M) return;
+    data_rows_body<T>(a, grid + jb.cell0, M, pl, tw + jb.tw0, work_b + jb.work0);
+}
+
+template <typename T>
+__global__ void k_bdata_cols(FftBatchMap m, const FftBatchJob *__restrict__ jobs,
+                             const typename Cx<T>::t *__restrict__ tw, const typename Cx<T>::t *__restrict__ work_b,
+                             const KSpec<T> *__restrict__ kspec, typename Cx<T>::t *__restrict__ work_a, int mode) {
+    const int j = m.job[blockIdx.x];
+    const FftBatchJob jb = jobs[j];
+    const int M = jb.cg->M;
+    const FftPlan pl = jb.cg->plan;
+    const int kb = (int) blockIdx.x - m.first[j];
+    if (kb >= pl.L / 2 + 1) return;
+    data_cols_body<T>(kb, M, pl, tw + jb.tw0, work_b + jb.work0, kspec + jb.kspec0, work_a + jb.work0, mode);
+}
+
+template <typename T>
+__global__ void k_bdata_rows_inv(FftBatchMap m, const FftBatchJob *__restrict__ jobs,
+                                 const typename Cx<T>::t *__restrict__ work_a, const typename Cx<T>::t *__restrict__ tw,
+                                 Cell4<T> *__restrict__ out) {
+    const int j = m.job[blockIdx.x];
+    const FftBatchJob jb = jobs[j];
+    const int M = jb.cg->M;
+    const FftPlan pl = jb.cg->plan;
+    const int a = (int) blockIdx.x - m.first[j];
+    if (a >= M) return;
+    data_rows_inv_body<T>(a, work_a + jb.work0, M, pl, tw + jb.tw0, out + jb.cell0);
+}
+
+// job blockIdx.y's twiddles for its current length
+template <typename T>
+__global__ void k_btwiddles(const FftBatchJob *__restrict__ jobs, typename Cx<T>::t *__restrict__ tw) {
+    const FftBatchJob jb = jobs[blockIdx.y];
+    const int L = jb.cg->plan.L;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L; k += gridDim.x * blockDim.x) {
+        double sn, cs;
+        sincospi(2.0 * (double) k / (double) L, &sn, &cs);
+        tw[jb.tw0 + k] = mkc((T) cs, (T) -sn);
+    }
+}
+}  // namespace
+
+template <typename T>
+cudaError_t conv2d_launch_batch(const Cell4<T> *grid_in, Cell4<T> *grid_out, const FftBatchJob *jobs,
+                                FftBatchMap krow, int nkrow, FftBatchMap cols, int ncols, FftBatchMap rows, int nrows,
+                                int L_max, const typename Cx<T>::t *tw, typename Cx<T>::t *work_a,
+                                typename Cx<T>::t *work_b, KSpec<T> *kspec, double df, int mode, cudaStream_t st) {
+    typedef typename Cx<T>::t C;
+    if (L_max > max_fft_len<T>()) return cudaErrorInvalidValue;
+    const size_t s4 = 4 * (size_t) L_max * sizeof(C);
+    const size_t s5 = 5 * (size_t) L_max * sizeof(C);
+    cudaError_t e;
+    if ((e = set_smem(k_bkernel_rows<T>, s4)) != cudaSuccess) return e;
+    if ((e = set_smem(k_bkernel_cols<T>, s5)) != cudaSuccess) return e;
+    if ((e = set_smem(k_bdata_rows<T>, s4)) != cudaSuccess) return e;
+    if ((e = set_smem(k_bdata_cols<T>, s5)) != cudaSuccess) return e;
+    if ((e = set_smem(k_bdata_rows_inv<T>, s4)) != cudaSuccess) return e;
+    const int thr = 256;
+    k_bkernel_rows<T><<<nkrow, thr, s4, st>>>(krow, jobs, tw, work_a, (T) df, mode);
+    k_bkernel_cols<T><<<ncols, thr, s5, st>>>(cols, jobs, tw, work_a, kspec);
+    k_bdata_rows<T><<<nrows, thr, s4, st>>>(rows, jobs, grid_in, tw, work_b);
+    k_bdata_cols<T><<<ncols, thr, s5, st>>>(cols, jobs, tw, work_b, kspec, work_a, mode);
+    k_bdata_rows_inv<T><<<nrows, thr, s4, st>>>(rows, jobs, work_a, tw, grid_out);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t twiddles_batch(const FftBatchJob *jobs, int J, typename Cx<T>::t *tw, cudaStream_t st) {
+    k_btwiddles<T><<<dim3(4, J), 256, 0, st>>>(jobs, tw);
+    return cudaGetLastError();
+}
+
+template cudaError_t conv2d_launch_batch<float>(const Cell4<float> *, Cell4<float> *, const FftBatchJob *,
+                                                FftBatchMap, int, FftBatchMap, int, FftBatchMap, int, int,
+                                                const float2 *, float2 *, float2 *, KSpec<float> *, double, int,
+                                                cudaStream_t);
+template cudaError_t twiddles_batch<float>(const FftBatchJob *, int, float2 *, cudaStream_t);
 
 template cudaError_t conv2d_launch<float>(const Cell4<float> *, Cell4<float> *, int, const FftPlan &, const float2 *,
                                           float2 *, float2 *, KSpec<float> *, double, double, int, cudaStream_t);

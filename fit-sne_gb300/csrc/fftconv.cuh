@@ -110,4 +110,27 @@ cudaError_t conv1d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
                           const typename Cx<T>::t *tw, typename Cx<T>::t *work, double h, double df, int mode,
                           cudaStream_t st);
 
+// Batched 2-D convolution (many embeddings, one launch per pass).  Job j's current geometry
+// is *jobs[j].cg (device), its grids / work buffers / spectra / twiddles start at the given
+// offsets of the concatenated arrays, sized for its capacity.  The blocks of each pass are
+// split among the jobs by a map (job of each block, first block of each job): kernel rows
+// (2 M_cap - 1 blocks per job), columns (L_cap / 2 + 1) and data rows (M_cap); blocks beyond
+// the job's current size return at once.  L_max: the largest capacity (shared memory).
+struct FftBatchJob {
+    const ConvGeom *cg;
+    size_t cell0, work0, kspec0, tw0;
+};
+struct FftBatchMap {
+    const int *job;
+    const int *first;
+};
+template <typename T>
+cudaError_t conv2d_launch_batch(const Cell4<T> *grid_in, Cell4<T> *grid_out, const FftBatchJob *jobs,
+                                FftBatchMap krow, int nkrow, FftBatchMap cols, int ncols, FftBatchMap rows, int nrows,
+                                int L_max, const typename Cx<T>::t *tw, typename Cx<T>::t *work_a,
+                                typename Cx<T>::t *work_b, KSpec<T> *kspec, double df, int mode, cudaStream_t st);
+// The twiddles of each job's current length (jobs[j].cg->plan.L) at tw + jobs[j].tw0.
+template <typename T>
+cudaError_t twiddles_batch(const FftBatchJob *jobs, int J, typename Cx<T>::t *tw, cudaStream_t st);
+
 }  // namespace fitsne

@@ -212,15 +212,15 @@ FITSNE_D void block_sum(double (&v)[NV], double *sh) {
 // Writes this block's partials; returns true in thread 0 of the last block to finish,
 // with v replaced by the total over all blocks (summed in block order).
 template <int NV>
-FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, double *sh) {
+FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, double *sh, int blk, int nblk) {
     block_sum<NV>(v, sh);
     __shared__ bool last;
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) part[blockIdx.x * NV + k] = v[k];
+        for (int k = 0; k < NV; ++k) part[blk * NV + k] = v[k];
         __threadfence();
         const unsigned int prev = atomicAdd(count, 1u);
-        last = (prev == gridDim.x - 1);
+        last = (prev == (unsigned int) nblk - 1);
     }
     __syncthreads();
     if (!last) return false;
@@ -228,7 +228,7 @@ FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, doubl
     double acc[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = 0.0;
-    for (int b = threadIdx.x; b < (int) gridDim.x; b += blockDim.x)
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] += ((volatile double *) part)[b * NV + k];
     block_sum<NV>(acc, sh);
@@ -243,7 +243,7 @@ FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, doubl
 
 // min / max with the same rule as the reference
 template <int NV>
-FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *count, double *sh) {
+FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *count, double *sh, int blk, int nblk) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int o = 16; o; o >>= 1) {
         mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
@@ -260,17 +260,17 @@ FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *co
             mn = fmin(mn, sh[2 * w]);
             mx = fmax(mx, sh[2 * w + 1]);
         }
-        part[2 * blockIdx.x] = mn;
-        part[2 * blockIdx.x + 1] = mx;
+        part[2 * blk] = mn;
+        part[2 * blk + 1] = mx;
         __threadfence();
         const unsigned int prev = atomicAdd(count, 1u);
-        last = (prev == gridDim.x - 1);
+        last = (prev == (unsigned int) nblk - 1);
     }
     __syncthreads();
     if (!last) return false;
     __threadfence();
     double a = HUGE_VAL, b = -HUGE_VAL;
-    for (int k = threadIdx.x; k < (int) gridDim.x; k += blockDim.x) {
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
         a = fmin(a, ((volatile double *) part)[2 * k]);
         b = fmax(b, ((volatile double *) part)[2 * k + 1]);
     }
@@ -300,9 +300,8 @@ FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *co
 // ---------------------------------------------------------------------------------
 // center (subtract the pending mean) + min/max (tsne.cpp:531, 1039-1049, 769-773)
 template <typename T, int D>
-__global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply_mean, int excl, RedScratch r) {
+FITSNE_D void center_minmax_body(T *Y, int N, int apply_mean, int excl, RedScratch r, double *sh, int blk, int nblk) {
     typedef typename YL<T, D>::P P;
-    __shared__ double sh[2 * 32];
     P negm[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -313,7 +312,7 @@ __global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply
             negm[d] = -m;
     }
     double mn = HUGE_VAL, mx = -HUGE_VAL;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    for (int i = blk * blockDim.x + threadIdx.x; i < N; i += nblk * blockDim.x) {
         P c[D];
         YL<T, D>::load(Y, i, c);
         if (apply_mean) {
@@ -330,10 +329,16 @@ __global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply
             if (!(D == 2 && i == excl && d == 0)) mn = fmin(mn, v);
         }
     }
-    if (grid_minmax<2>(mn, mx, r.part, r.count + 0, sh)) {
+    if (grid_minmax<2>(mn, mx, r.part, r.count + 0, sh, blk, nblk)) {
         r.mnmx[0] = mn;
         r.mnmx[1] = mx;
     }
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(kBlock) k_center_minmax(T *Y, int N, int apply_mean, int excl, RedScratch r) {
+    __shared__ double sh[2 * 32];
+    center_minmax_body<T, D>(Y, N, apply_mean, excl, r, sh, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -390,17 +395,15 @@ __global__ void __launch_bounds__(kBlock) k_spread(const T *__restrict__ Y, int 
 // sums in its last lane, which alone issues the node atomics.  Identical charges to
 // k_spread; only the order of the FP32 additions differs.
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_spread_runs(const float *__restrict__ Y, int N, BoxP<float> b,
-                                                        Cell4<float> *__restrict__ grid,
-                                                        const DevGeom *__restrict__ dg) {
+FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<float> &b,
+                               Cell4<float> *__restrict__ grid, int blk, int nblk) {
     constexpr int NT = 3;
-    if (dg) b = make_box(dg->g, (float *) nullptr);
     constexpr int NV = (D == 2) ? NT * NT : NT;  // nodes per point
     constexpr int NC = (D == 2) ? 4 : 3;         // charge values per node
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int warp0 = (blk * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (nblk * blockDim.x) >> 5;
     for (int base = warp0 * 32; base < N; base += nwarps * 32) {
         const int i = base + lane;
         const bool valid = i < N;
@@ -491,19 +494,24 @@ __global__ void __launch_bounds__(kBlock) k_spread_runs(const float *__restrict_
     }
 }
 
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_spread_runs(const float *__restrict__ Y, int N, BoxP<float> b,
+                                                        Cell4<float> *__restrict__ grid,
+                                                        const DevGeom *__restrict__ dg) {
+    if (dg) b = make_box(dg->g, (float *) nullptr);
+    spread_runs_body<D>(Y, N, b, grid, blockIdx.x, gridDim.x);
+}
+
 // ---------------------------------------------------------------------------------
 // gather (step 3) + the repulsion numerators + Z
 template <typename T, int D, int NT>
-__global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int N, BoxP<T> b,
-                                                   const Cell4<T> *__restrict__ pot, int mode,
-                                                   T *__restrict__ rep, RedScratch r,
-                                                   const DevGeom *__restrict__ dg, float *__restrict__ yh) {
+FITSNE_D void gather_body(const T *__restrict__ Y, int N, const BoxP<T> &b, const Cell4<T> *__restrict__ pot,
+                          int mode, T *__restrict__ rep, RedScratch r, float *__restrict__ yh, double *sh, int blk,
+                          int nblk) {
     typedef typename YL<T, D>::P P;
-    if (dg) b = make_box(dg->g, (T *) nullptr);
-    __shared__ double sh[32];
     const int n = NT > 0 ? NT : b.nterms;
     double zacc[1] = {0.0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    for (int i = blk * blockDim.x + threadIdx.x; i < N; i += nblk * blockDim.x) {
         P c[D];
         YL<T, D>::load(Y, i, c);
         if constexpr (sizeof(T) == 4) {
@@ -558,7 +566,17 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
         }
         zacc[0] += (double) zi;
     }
-    if (grid_sum<1>(zacc, r.part, r.count + 1, sh)) *r.z = zacc[0] - (double) N;
+    if (grid_sum<1>(zacc, r.part, r.count + 1, sh, blk, nblk)) *r.z = zacc[0] - (double) N;
+}
+
+template <typename T, int D, int NT>
+__global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int N, BoxP<T> b,
+                                                   const Cell4<T> *__restrict__ pot, int mode,
+                                                   T *__restrict__ rep, RedScratch r,
+                                                   const DevGeom *__restrict__ dg, float *__restrict__ yh) {
+    __shared__ double sh[32];
+    if (dg) b = make_box(dg->g, (T *) nullptr);
+    gather_body<T, D, NT>(Y, N, b, pot, mode, rep, r, yh, sh, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -625,7 +643,7 @@ FITSNE_D void attr_row_update(int my, const T (&amy)[D], const typename YL<T, D>
 // in mode 1 the grid sum of the new positions gives the mean that the next centring removes.
 template <typename T, int D>
 FITSNE_D void attr_finish(int lane, unsigned int nwarps, int N, const UpdateParams &p, RedScratch r,
-                          const typename YL<T, D>::P (&msum)[D], double *sh) {
+                          const typename YL<T, D>::P (&msum)[D], double *sh, int blk, int nblk) {
     if (lane == 0) {
         __threadfence();
         const unsigned int out = atomicAdd(r.count + 5, 1u);
@@ -638,7 +656,7 @@ FITSNE_D void attr_finish(int lane, unsigned int nwarps, int N, const UpdatePara
         double m[2] = {0.0, 0.0};
 #pragma unroll
         for (int d = 0; d < D; ++d) m[d] = ptod(msum[d]);
-        if (grid_sum<2>(m, r.part, r.count + 2, sh)) {
+        if (grid_sum<2>(m, r.part, r.count + 2, sh, blk, nblk)) {
             r.mean[0] = m[0] / (double) N;
             r.mean[1] = m[1] / (double) N;
         }
@@ -656,19 +674,19 @@ FITSNE_D void attr_finish(int lane, unsigned int nwarps, int N, const UpdatePara
 // remain: the CSR entries (prefetched into L2 while the previous row is processed) and the
 // neighbour Y gathers (L2-resident).  Within a row, lanes take kAttrUnroll edges each per
 // batch: all index / value loads first, then all gathers.
-template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups = false, bool kPipe = false,
-          int kMinBlocks = 1>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
-                                                 const T *__restrict__ val, const T *__restrict__ Yin,
-                                                 T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
-                                                 T *__restrict__ dC, const T *__restrict__ rep, int N,
-                                                 UpdateParams p, RedScratch r, const float *__restrict__ yh) {
+// Rows [row0, row0 + N) of the CSR (column indices and Y are global); blk / nblk: this
+// block's index among the nblk blocks that share the rows (and r's counters).
+template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups, bool kPipe>
+FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                        const T *__restrict__ val, const T *__restrict__ Yin, T *__restrict__ Yout,
+                        T *__restrict__ uY, T *__restrict__ gains, T *__restrict__ dC, const T *__restrict__ rep,
+                        int row0, int N, const UpdateParams &p, RedScratch r, const float *__restrict__ yh,
+                        double *sh, int *block_item, int blk, int nblk) {
     typedef typename YL<T, D>::P P;
-    __shared__ double sh[2 * 32];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int ngroups = (N + kAttrGroup - 1) / kAttrGroup;
-    const unsigned int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned int nwarps = (nblk * blockDim.x) >> 5;
     const double Zd = *r.z;
     const T zinv = T(1.0 / Zd);
     const T df = T(p.df);
@@ -682,24 +700,23 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__r
         else
             msum[d] = 0.0;
     }
-    __shared__ int block_item;
     while (true) {
         int g = 0;
         if constexpr (kBlockGroups) {
             __syncthreads();  // every warp has read the previous item
-            if (threadIdx.x == 0) block_item = (int) atomicAdd(r.count + 4, 1u);
+            if (threadIdx.x == 0) *block_item = (int) atomicAdd(r.count + 4, 1u);
             __syncthreads();
             const int wpb = blockDim.x >> 5;
-            if (block_item * wpb >= ngroups) break;  // uniform over the block
-            g = block_item * wpb + (threadIdx.x >> 5);
+            if (*block_item * wpb >= ngroups) break;  // uniform over the block
+            g = *block_item * wpb + (threadIdx.x >> 5);
             if (g >= ngroups) continue;
         } else {
             if (lane == 0) g = (int) atomicAdd(r.count + 4, 1u);
             g = __shfl_sync(full, g, 0);
             if (g >= ngroups) break;
         }
-        const int i0 = g * kAttrGroup;
-        const int nr = min(kAttrGroup, N - i0);
+        const int i0 = row0 + g * kAttrGroup;
+        const int nr = min(kAttrGroup, row0 + N - i0);
         const int my = i0 + lane;
         const bool live = lane < nr;
         const uint32_t rb = live ? row[my] : 0u;
@@ -821,25 +838,37 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__r
         if (!live) continue;
         attr_row_update<T, D>(my, amy, cmy, p, zinv, exag, rep, dC, gains, uY, Yout, msum);
     }
-    attr_finish<T, D>(lane, nwarps, N, p, r, msum, sh);
+    attr_finish<T, D>(lane, nwarps, N, p, r, msum, sh, blk, nblk);
+}
+
+template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups = false, bool kPipe = false,
+          int kMinBlocks = 1>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_attr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                                                 const T *__restrict__ val, const T *__restrict__ Yin,
+                                                 T *__restrict__ Yout, T *__restrict__ uY, T *__restrict__ gains,
+                                                 T *__restrict__ dC, const T *__restrict__ rep, int N,
+                                                 UpdateParams p, RedScratch r, const float *__restrict__ yh) {
+    __shared__ double sh[2 * 32];
+    __shared__ int block_item;
+    attr_body<T, D, kAttrGroup, kAttrUnroll, kBlockGroups, kPipe>(row, col, val, Yin, Yout, uY, gains, dC, rep, 0, N,
+                                                                  p, r, yh, sh, &block_item, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------------
 // KL divergence over the CSR edges (evaluateErrorFft, tsne.cpp:1329-1355)
 template <typename T, int D>
-__global__ void __launch_bounds__(kBlock) k_kl(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
-                                               const T *__restrict__ val, const T *__restrict__ Y, int N,
-                                               double exag, double dfd, RedScratch r) {
+FITSNE_D void kl_body(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col, const T *__restrict__ val,
+                      const T *__restrict__ Y, int row0, int N, double exag, double dfd, RedScratch r, double *sh,
+                      int blk, int nblk) {
     typedef typename YL<T, D>::P P;
-    __shared__ double sh[32];
     const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int gw = (blk * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (nblk * blockDim.x) >> 5;
     const T zinv = T(1.0 / *r.z);
     const T df = T(dfd);
     const T ex = T(exag);
     double acc[1] = {0.0};
-    for (int i = gw; i < N; i += nw) {
+    for (int i = row0 + gw; i < row0 + N; i += nw) {
         P ci[D];
         YL<T, D>::load(Y, i, ci);
         const uint32_t e1 = row[i + 1];
@@ -858,7 +887,15 @@ __global__ void __launch_bounds__(kBlock) k_kl(const uint32_t *__restrict__ row,
             acc[0] += (double) (pv * log((pv + T(FLT_MIN)) / (Q + T(FLT_MIN))));
         }
     }
-    if (grid_sum<1>(acc, r.part, r.count + 3, sh)) *r.kl = acc[0];
+    if (grid_sum<1>(acc, r.part, r.count + 3, sh, blk, nblk)) *r.kl = acc[0];
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(kBlock) k_kl(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                                               const T *__restrict__ val, const T *__restrict__ Y, int N,
+                                               double exag, double dfd, RedScratch r) {
+    __shared__ double sh[32];
+    kl_body<T, D>(row, col, val, Y, 0, N, exag, dfd, r, sh, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -989,9 +1026,8 @@ namespace {
 // (the host rule of make_grid_geom, in the same FP64 operations) and ORs its status into
 // *status_acc.  A grid above the capacity is clamped to it so that every kernel stays in
 // its buffers; the iteration is then void and the caller repeats it with a larger one.
-__global__ void k_geometry(RedScratch r, int D, int nterms, double ipi, int min_num, int nb_cap, int L_cap,
-                           DevGeom *__restrict__ dg, int *__restrict__ status_acc) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+FITSNE_D void geometry_one(const RedScratch &r, int D, int nterms, double ipi, int min_num, int nb_cap, int L_cap,
+                          DevGeom *__restrict__ dg, int *__restrict__ status_acc) {
     double mn = r.mnmx[0], mx = r.mnmx[1];
     int status = 0;
     if (!isfinite(mn) || !isfinite(mx)) {
@@ -1015,6 +1051,12 @@ __global__ void k_geometry(RedScratch r, int D, int nterms, double ipi, int min_
     make_fft_plan(L, &dg->conv.plan);
     dg->status = status;
     if (status) atomicOr(status_acc, status == 2 ? 2 : 1);
+}
+
+__global__ void k_geometry(RedScratch r, int D, int nterms, double ipi, int min_num, int nb_cap, int L_cap,
+                           DevGeom *__restrict__ dg, int *__restrict__ status_acc) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    geometry_one(r, D, nterms, ipi, min_num, nb_cap, L_cap, dg, status_acc);
 }
 }  // namespace
 
@@ -1118,6 +1160,150 @@ cudaError_t launch_cast_from_double(const double *src, T *dst, size_t n, cudaStr
     const int g = grid_for((long long) n, kBlock, 8192);
     k_cast<T><<<g, kBlock, 0, st>>>(src, dst, n);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// Batched stages: a thin wrapper per stage finds the block's job and runs the single-job body
+// on that job's slice of the concatenated arrays, with the job's own geometry and reduction
+// scratch, over the job's share of the launch's blocks.
+namespace {
+constexpr int kBatchGroup = 16;   // attraction: rows per work item
+constexpr int kBatchUnroll = 2;   //             edges per lane per batch
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_bcenter(float *Y, BatchMap m, const BatchJobDev *__restrict__ jobs,
+                                                    const RedScratch *__restrict__ rs, int apply_mean) {
+    __shared__ double sh[2 * 32];
+    const int j = m.job[blockIdx.x];
+    const BatchJobDev jb = jobs[j];
+    // excl = 0: the job's first point (the batched form keeps the caller's numbering)
+    center_minmax_body<float, D>(Y + (size_t) jb.p0 * (2 * D), jb.n, apply_mean, 0, rs[j], sh,
+                                 (int) blockIdx.x - m.first[j], m.count[j]);
+}
+
+__global__ void k_bgeometry(const RedScratch *__restrict__ rs, const BatchJobDev *__restrict__ jobs, int J, int D,
+                            int nterms, double ipi, int min_num, DevGeom *__restrict__ dg, int *__restrict__ status) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J) return;
+    geometry_one(rs[j], D, nterms, ipi, min_num, jobs[j].nb_cap, jobs[j].L_cap, &dg[j], &status[j]);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_bspread(const float *__restrict__ Y, BatchMap m,
+                                                    const BatchJobDev *__restrict__ jobs,
+                                                    const DevGeom *__restrict__ dg, Cell4<float> *__restrict__ grid) {
+    const int j = m.job[blockIdx.x];
+    const BatchJobDev jb = jobs[j];
+    const BoxP<float> b = make_box(dg[j].g, (float *) nullptr);
+    spread_runs_body<D>(Y + (size_t) jb.p0 * (2 * D), jb.n, b, grid + jb.cell0, (int) blockIdx.x - m.first[j],
+                        m.count[j]);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_bgather(const float *__restrict__ Y, BatchMap m,
+                                                    const BatchJobDev *__restrict__ jobs,
+                                                    const DevGeom *__restrict__ dg,
+                                                    const Cell4<float> *__restrict__ pot, float *__restrict__ rep,
+                                                    const RedScratch *__restrict__ rs, float *__restrict__ yh) {
+    __shared__ double sh[32];
+    const int j = m.job[blockIdx.x];
+    const BatchJobDev jb = jobs[j];
+    const BoxP<float> b = make_box(dg[j].g, (float *) nullptr);
+    gather_body<float, D, 3>(Y + (size_t) jb.p0 * (2 * D), jb.n, b, pot + jb.cell0, KERNEL_DF1,
+                             rep + (size_t) jb.p0 * D, rs[j], yh + (size_t) jb.p0 * D, sh,
+                             (int) blockIdx.x - m.first[j], m.count[j]);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_battr(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                                                  const float *__restrict__ val, const float *__restrict__ Yin,
+                                                  float *__restrict__ Yout, float *__restrict__ uY,
+                                                  float *__restrict__ gains, const float *__restrict__ rep,
+                                                  BatchMap m, const BatchJobDev *__restrict__ jobs,
+                                                  const RedScratch *__restrict__ rs, UpdateParams p,
+                                                  const float *__restrict__ yh) {
+    __shared__ double sh[2 * 32];
+    __shared__ int block_item;
+    const int j = m.job[blockIdx.x];
+    const BatchJobDev jb = jobs[j];
+    p.learning_rate = jb.lr;
+    attr_body<float, D, kBatchGroup, kBatchUnroll, false, false>(row, col, val, Yin, Yout, uY, gains, nullptr, rep,
+                                                                 jb.p0, jb.n, p, rs[j], yh, sh, &block_item,
+                                                                 (int) blockIdx.x - m.first[j], m.count[j]);
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_bkl(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
+                                                const float *__restrict__ val, const float *__restrict__ Y,
+                                                BatchMap m, const BatchJobDev *__restrict__ jobs, double exag,
+                                                const RedScratch *__restrict__ rs) {
+    __shared__ double sh[32];
+    const int j = m.job[blockIdx.x];
+    const BatchJobDev jb = jobs[j];
+    kl_body<float, D>(row, col, val, Y, jb.p0, jb.n, exag, 1.0, rs[j], sh, (int) blockIdx.x - m.first[j],
+                      m.count[j]);
+}
+}  // namespace
+
+cudaError_t launch_batch_center(float *Y, int D, BatchMap m, int nblocks, const BatchJobDev *jobs,
+                                const RedScratch *rs, int apply_mean, cudaStream_t st) {
+    if (D == 2)
+        k_bcenter<2><<<nblocks, kBlock, 0, st>>>(Y, m, jobs, rs, apply_mean);
+    else
+        k_bcenter<1><<<nblocks, kBlock, 0, st>>>(Y, m, jobs, rs, apply_mean);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_geometry(const RedScratch *rs, const BatchJobDev *jobs, int J, int D, int nterms,
+                                  double ipi, int min_num, DevGeom *dg, int *status, cudaStream_t st) {
+    k_bgeometry<<<(J + 31) / 32, 32, 0, st>>>(rs, jobs, J, D, nterms, ipi, min_num, dg, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_spread(const float *Y, int D, BatchMap m, int nblocks, const BatchJobDev *jobs,
+                                const DevGeom *dg, Cell4<float> *grid, cudaStream_t st) {
+    if (D == 2)
+        k_bspread<2><<<nblocks, kBlock, 0, st>>>(Y, m, jobs, dg, grid);
+    else
+        k_bspread<1><<<nblocks, kBlock, 0, st>>>(Y, m, jobs, dg, grid);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_gather(const float *Y, int D, BatchMap m, int nblocks, const BatchJobDev *jobs,
+                                const DevGeom *dg, const Cell4<float> *pot, float *rep, const RedScratch *rs,
+                                float *yh, cudaStream_t st) {
+    if (D == 2)
+        k_bgather<2><<<nblocks, kBlock, 0, st>>>(Y, m, jobs, dg, pot, rep, rs, yh);
+    else
+        k_bgather<1><<<nblocks, kBlock, 0, st>>>(Y, m, jobs, dg, pot, rep, rs, yh);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_attr(const uint32_t *row, const uint32_t *col, const float *val, const float *Yin,
+                              float *Yout, float *uY, float *gains, const float *rep, int D, BatchMap m,
+                              int nblocks, const BatchJobDev *jobs, const RedScratch *rs, const UpdateParams &p,
+                              const float *yh, cudaStream_t st) {
+    if (D == 2)
+        k_battr<2><<<nblocks, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, rep, m, jobs, rs, p, yh);
+    else
+        k_battr<1><<<nblocks, kBlock, 0, st>>>(row, col, val, Yin, Yout, uY, gains, rep, m, jobs, rs, p, yh);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_kl(const uint32_t *row, const uint32_t *col, const float *val, const float *Y, int D,
+                            BatchMap m, int nblocks, const BatchJobDev *jobs, double exag, const RedScratch *rs,
+                            cudaStream_t st) {
+    if (D == 2)
+        k_bkl<2><<<nblocks, kBlock, 0, st>>>(row, col, val, Y, m, jobs, exag, rs);
+    else
+        k_bkl<1><<<nblocks, kBlock, 0, st>>>(row, col, val, Y, m, jobs, exag, rs);
+    return cudaGetLastError();
+}
+
+int batch_attr_blocks_per_sm() {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_battr<2>, kBlock, 0) != cudaSuccess) return 1;
+    return per_sm > 0 ? per_sm : 1;
 }
 
 #define FITSNE_INST(T)                                                                                           \

@@ -103,6 +103,22 @@ struct DevGeom {
     int status;
 };
 
+// ---- batched form: many embeddings ("jobs") in concatenated arrays, one launch per stage ----
+// The blocks of a batched launch are split among the jobs: job[b] is the job of block b,
+// first[j] and count[j] the first block and the number of blocks of job j (device arrays).
+struct BatchMap {
+    const int *job;
+    const int *first;
+    const int *count;
+};
+// One job of the batched iteration (device table).
+struct BatchJobDev {
+    int p0, n;          // its points: [p0, p0 + n) of the concatenated arrays (CSR rows too)
+    int nb_cap, L_cap;  // grid capacity: boxes per dimension and FFT length
+    size_t cell0;       // its first cell of the concatenated grids (capacity (nb_cap nterms)^2)
+    float lr;           // learning rate
+};
+
 // Reduction scratch shared by the kernels of one embedding (device memory).
 struct RedScratch {
     double *part;          // per-block partials, up to kMaxRedBlocks * 4 doubles
@@ -159,6 +175,27 @@ cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T
 template <typename T>
 cudaError_t launch_kl(const uint32_t *row, const uint32_t *col, const T *val, const T *Y, int N, int D, double exag,
                       double df, RedScratch r, cudaStream_t st);
+// Batched stages (FP32 form, nterms 3, df = 1).  Each job reduces over its own blocks into its
+// own RedScratch rs[j]; Y, rep, yh, uY, gains and the CSR are the concatenated arrays.
+cudaError_t launch_batch_center(float *Y, int D, BatchMap m, int nblocks, const BatchJobDev *jobs,
+                                const RedScratch *rs, int apply_mean, cudaStream_t st);
+cudaError_t launch_batch_geometry(const RedScratch *rs, const BatchJobDev *jobs, int J, int D, int nterms,
+                                  double ipi, int min_num, DevGeom *dg, int *status, cudaStream_t st);
+cudaError_t launch_batch_spread(const float *Y, int D, BatchMap m, int nblocks, const BatchJobDev *jobs,
+                                const DevGeom *dg, Cell4<float> *grid, cudaStream_t st);
+cudaError_t launch_batch_gather(const float *Y, int D, BatchMap m, int nblocks, const BatchJobDev *jobs,
+                                const DevGeom *dg, const Cell4<float> *pot, float *rep, const RedScratch *rs,
+                                float *yh, cudaStream_t st);
+cudaError_t launch_batch_attr(const uint32_t *row, const uint32_t *col, const float *val, const float *Yin,
+                              float *Yout, float *uY, float *gains, const float *rep, int D, BatchMap m,
+                              int nblocks, const BatchJobDev *jobs, const RedScratch *rs, const UpdateParams &p,
+                              const float *yh, cudaStream_t st);
+cudaError_t launch_batch_kl(const uint32_t *row, const uint32_t *col, const float *val, const float *Y, int D,
+                            BatchMap m, int nblocks, const BatchJobDev *jobs, double exag, const RedScratch *rs,
+                            cudaStream_t st);
+// Blocks the batched attraction may keep resident per SM (for sizing its launch).
+int batch_attr_blocks_per_sm();
+
 // host <-> device Y conversion (double array N*D <-> storage layout)
 template <typename T>
 cudaError_t launch_y_from_double(const double *src, T *Y, int N, int D, cudaStream_t st);

@@ -11,6 +11,7 @@
 
 #include "../../include/fitsne_gb300.h"
 #include "affinity.cuh"
+#include "batch.cuh"
 #include "capi_internal.h"
 #include "embedding.cuh"
 #include "knn.cuh"
@@ -602,6 +603,61 @@ int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int 
     int rc = check_cuda_device();
     if (rc) return rc;
     const auto t0 = std::chrono::steady_clock::now();
+    GridParams gp;
+    gp.nterms = nterms;
+    gp.intervals_per_integer = intervals_per_integer;
+    gp.min_num_intervals = min_num_intervals;
+    gp.df = 1.0;
+    Schedule s;
+    s.max_iter = max_iter;
+    s.stop_lying_iter = stop_lying_iter;
+    s.mom_switch_iter = mom_switch_iter;
+    s.momentum = momentum;
+    s.final_momentum = final_momentum;
+    s.early_exag_coeff = early_exag_coeff;
+    s.max_step_norm = max_step_norm;
+    std::vector<double> lr(learning_rate, learning_rate + njobs);
+    const char *bmode = std::getenv("FITSNE_BATCH");  // "streams": one graph per job on its own stream
+    if (BatchPipeline::supports(no_dims, gp) && !(bmode && std::string(bmode) == "streams")) {
+        // every job in the same launches (batch.cuh)
+        Stream st;
+        std::vector<DevCSR> Ps(njobs);
+        struct FreeP {
+            std::vector<DevCSR> &v;
+            ~FreeP() {
+                for (auto &p : v) free_csr(p);
+            }
+        } free_p{Ps};
+        std::vector<const double *> Y0(njobs);
+        for (int j = 0; j < njobs; ++j) {
+            rc = build_P(X[j], N[j], D[j], perplexity[j], -1, -1.0, 0, nullptr, &Ps[j], st.s, false, false);
+            if (rc) return rc;
+            if (!skip_random_init) {
+                std::srand(rand_seed ? (unsigned int) rand_seed[j] : 0u);
+                for (size_t i = 0; i < (size_t) N[j] * no_dims; ++i) Y[j][i] = randn_polar() * .0001;
+            }
+            Y0[j] = Y[j];
+        }
+        BatchPipeline bp;
+        rc = bp.init(Ps, Y0, lr, gp, st.s);
+        for (auto &p : Ps) free_csr(p);
+        if (rc) return set_error(FITSNE_E_CUDA, bp.error());
+        const auto t1 = std::chrono::steady_clock::now();
+        double bs[5] = {0, 0, 0, 0, 0};
+        rc = bp.run_schedule(s, costs, bs);
+        if (rc) return set_error(rc == -11 ? FITSNE_E_GRID : FITSNE_E_CUDA, bp.error());
+        for (int j = 0; j < njobs; ++j)
+            if (bp.get_Y(j, Y[j])) return set_error(FITSNE_E_CUDA, bp.error());
+        const auto t2 = std::chrono::steady_clock::now();
+        if (stats5) {
+            stats5[0] = std::chrono::duration<double>(t1 - t0).count();
+            stats5[1] = std::chrono::duration<double>(t2 - t1).count();
+            stats5[2] = bs[0];
+            stats5[3] = bs[1] - bs[2];  // instantiations (the rest were in-place updates)
+            stats5[4] = bs[3];
+        }
+        return 0;
+    }
     std::vector<std::unique_ptr<BatchJob>> jobs;
     for (int j = 0; j < njobs; ++j) {
         jobs.emplace_back(new BatchJob());
@@ -618,11 +674,6 @@ int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int 
             }
         }
     } cleanup{jobs};
-    GridParams gp;
-    gp.nterms = nterms;
-    gp.intervals_per_integer = intervals_per_integer;
-    gp.min_num_intervals = min_num_intervals;
-    gp.df = 1.0;
     // similarities and initial embeddings, job by job
     for (int j = 0; j < njobs; ++j) {
         DevCSR P;
@@ -637,15 +688,6 @@ int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int 
         if (rc) return set_error(FITSNE_E_CUDA, jobs[j]->emb.error());
     }
     const auto t1 = std::chrono::steady_clock::now();
-    Schedule s;
-    s.max_iter = max_iter;
-    s.stop_lying_iter = stop_lying_iter;
-    s.mom_switch_iter = mom_switch_iter;
-    s.momentum = momentum;
-    s.final_momentum = final_momentum;
-    s.early_exag_coeff = early_exag_coeff;
-    s.max_step_norm = max_step_norm;
-    std::vector<double> lr(learning_rate, learning_rate + njobs);
     double st5[5] = {0, 0, 0, 0, 0};
     rc = batch_iterate(jobs, s, lr, costs, st5);
     if (rc) return rc;

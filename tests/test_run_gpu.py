@@ -147,11 +147,16 @@ def test_graph_iteration_matches_host_iteration_fp64(gpu_lib, monkeypatch, golde
     assert np.abs(Ya - Yb).max() <= 1e-6 * np.abs(Ya).max()
 
 
-def test_batched_jobs_match_single_runs(gpu_lib):
+@pytest.mark.parametrize("mode", ["pipeline", "streams"])
+def test_batched_jobs_match_single_runs(gpu_lib, monkeypatch, mode):
     """fitsne_batch_run advances several embeddings together; each job ends where its own
     fitsne_run ends (final KL within 1%), the 5,000-point job within 1% of the reference.
+    "pipeline": all jobs in the same launches (the default for 2-D, nterms 3, df 1);
+    "streams": one graph per job on its own stream (FITSNE_BATCH=streams).
     (Clustered data: on structureless data the final KL of two FP32 runs differs by the
     optimiser's chaos alone, 1.2% on 1,200 isotropic Gaussian points.)"""
+    if mode == "streams":
+        monkeypatch.setenv("FITSNE_BATCH", "streams")
     m, g = _kl5000()
     X5, Y5 = m.data()
     rng = np.random.default_rng(3)
