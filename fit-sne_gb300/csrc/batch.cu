@@ -245,7 +245,7 @@ int BatchPipeline::upload_maps() {
     size_t pj, pf, pc, aj, af, ac, kj, kf, kc, cj, cf, cc, rj, rf, rc;
     n_pp_ = build([&](int j) { return pp_blocks(n_[j]); }, pj, pf, pc);
     n_at_ = build([&](int j) { return at_blocks(n_[j]); }, aj, af, ac);
-    n_krow_ = build([&](int j) { return 2 * nb_cap_[j] * gp_.nterms - 1; }, kj, kf, kc);
+    n_krow_ = build([&](int j) { return nb_cap_[j] * gp_.nterms; }, kj, kf, kc);
     n_cols_ = build([&](int j) { return hjobs_[j].L_cap / 2 + 1; }, cj, cf, cc);
     n_rows_ = build([&](int j) { return nb_cap_[j] * gp_.nterms; }, rj, rf, rc);
     if (host.size() > maps_len_) {

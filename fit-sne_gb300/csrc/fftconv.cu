@@ -211,8 +211,10 @@ FITSNE_D void kernel_rows_body(int r, int M, const FftPlan &pl, const typename C
     const int L = pl.L, H = L / 2 + 1;
     C *bufa = reinterpret_cast<C *>(smem_raw);
     C *bufb = bufa + 2 * L;
-    const int a = (r < M) ? r : (L - (2 * M - 1 - r));
-    const int dx = (a < M) ? a : a - L;
+    // rows dx = r >= 0 only: the fields are even in dx (K, Gy, H) or odd (Gx), so the
+    // column pass reads row -dx as +-row dx
+    const int a = r;
+    const int dx = r;
     for (int b = threadIdx.x; b < L; b += blockDim.x) {
         T k = 0, gx = 0, gy = 0, hh = 0;
         if (b < M || b > L - M) {
@@ -243,7 +245,7 @@ __global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__rest
         M = cg->M;
         pl = cg->plan;
         h = (T) cg->h;
-        if ((int) blockIdx.x >= 2 * M - 1) return;
+        if ((int) blockIdx.x >= M) return;
     }
     kernel_rows_body<T>(blockIdx.x, M, pl, tw, krow, h, df, mode);
 }
@@ -251,31 +253,38 @@ __global__ void k_kernel_rows(int M, FftPlan pl, const typename Cx<T>::t *__rest
 template <typename T>
 FITSNE_D void kernel_cols_body(int kb, int M, const FftPlan &pl, const typename Cx<T>::t *__restrict__ tw,
                                const typename Cx<T>::t *__restrict__ krow, KSpec<T> *__restrict__ kspec) {
+    // The row spectra are real for K, Gx and H (even in dy) and imaginary for Gy (odd in dy);
+    // as functions of dx, K, Gy and H are even and Gx is odd.  So one complex column FFT
+    // carries K + i H (both outputs real: the real and imaginary parts) and another Gx + i Gy/i
+    // (Gx's output imaginary and odd, Gy's real and even: split by the even / odd parts of
+    // the imaginary output at k and L - k).
     typedef typename Cx<T>::t C;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = pl.L, H = L / 2 + 1;
-    C *spec = reinterpret_cast<C *>(smem_raw);
-    C *scratch = spec + 4 * L;
-    for (int f = 0; f < 4; ++f)
-        for (int a = threadIdx.x; a < L; a += blockDim.x) {
-            const bool valid = (a < M) || (a > L - M);
-            spec[f * L + a] = valid ? krow[((size_t) f * L + a) * H + kb] : mkc(T(0), T(0));
+    C *z = reinterpret_cast<C *>(smem_raw);
+    C *scratch = z + 2 * L;
+    for (int a = threadIdx.x; a < L; a += blockDim.x) {
+        C z1 = mkc(T(0), T(0)), z2 = mkc(T(0), T(0));
+        const int idx = (a < M) ? a : ((a > L - M) ? L - a : -1);
+        if (idx >= 0) {
+            const T sgn = (a < M) ? T(1) : T(-1);  // Gx is odd in dx
+            z1 = mkc(krow[((size_t) 0 * L + idx) * H + kb].x, krow[((size_t) 3 * L + idx) * H + kb].x);
+            z2 = mkc(sgn * krow[((size_t) 1 * L + idx) * H + kb].x, krow[((size_t) 2 * L + idx) * H + kb].y);
         }
-    __syncthreads();
-    for (int f = 0; f < 4; ++f) {
-        C *res = fft_block(spec + f * L, scratch, 1, pl, tw, false);
-        if (res != spec + f * L) {
-            for (int a = threadIdx.x; a < L; a += blockDim.x) spec[f * L + a] = res[a];
-            __syncthreads();
-        }
+        z[a] = z1;
+        z[L + a] = z2;
     }
+    __syncthreads();
+    const C *res = fft_block(z, scratch, 2, pl, tw, false);
     const T s = T(1) / (T(L) * T(L));
     for (int ka = threadIdx.x; ka < L; ka += blockDim.x) {
+        const int km = ka ? L - ka : 0;
+        const T i2 = res[L + ka].y, i2m = res[L + km].y;
         KSpec<T> e;
-        e.k = spec[ka].x * s;
-        e.gx = spec[L + ka].y * s;
-        e.gy = spec[2 * L + ka].y * s;
-        e.h = spec[3 * L + ka].x * s;
+        e.k = res[ka].x * s;
+        e.h = res[ka].y * s;
+        e.gx = T(0.5) * (i2 - i2m) * s;
+        e.gy = T(0.5) * (i2 + i2m) * s;
         kspec[(size_t) kb * L + ka] = e;
     }
 }
@@ -548,7 +557,7 @@ cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
     if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
     const int thr = 256;
     // kernel spectra: krow uses work_a ([4][L][H]); data passes use work_b ([4][M][H]) then work_a
-    k_kernel_rows<T><<<2 * M - 1, thr, s4, st>>>(M, plan, tw, work_a, (T) h, (T) df, mode, nullptr);
+    k_kernel_rows<T><<<M, thr, s4, st>>>(M, plan, tw, work_a, (T) h, (T) df, mode, nullptr);
     k_kernel_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_a, kspec, nullptr);
     k_data_rows<T><<<M, thr, s4, st>>>(grid_in, M, plan, tw, work_b, nullptr);
     k_data_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_b, kspec, work_a, mode, nullptr);
@@ -573,7 +582,7 @@ cudaError_t conv2d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M
     if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
     const int thr = 256;
     FftPlan dummy{};
-    k_kernel_rows<T><<<2 * M_cap - 1, thr, s4, st>>>(0, dummy, tw, work_a, T(0), (T) df, mode, cg);
+    k_kernel_rows<T><<<M_cap, thr, s4, st>>>(0, dummy, tw, work_a, T(0), (T) df, mode, cg);
     k_kernel_cols<T><<<H, thr, s5, st>>>(0, dummy, tw, work_a, kspec, cg);
     k_data_rows<T><<<M_cap, thr, s4, st>>>(grid_in, 0, dummy, tw, work_b, cg);
     k_data_cols<T><<<H, thr, s5, st>>>(0, dummy, tw, work_b, kspec, work_a, mode, cg);
@@ -642,7 +651,7 @@ __global__ void k_bkernel_rows(FftBatchMap m, const FftBatchJob *__restrict__ jo
     const int M = jb.cg->M;
     const FftPlan pl = jb.cg->plan;
     const int r = (int) blockIdx.x - m.first[j];
-    if (r >= 2 * M - 1) return;
+    if (r >= M) return;
     kernel_rows_body<T>(r, M, pl, tw + jb.tw0, work_a + jb.work0, (T) jb.cg->h, df, mode);
 }
 

@@ -114,7 +114,7 @@ cudaError_t conv1d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
 // is *jobs[j].cg (device), its grids / work buffers / spectra / twiddles start at the given
 // offsets of the concatenated arrays, sized for its capacity.  The blocks of each pass are
 // split among the jobs by a map (job of each block, first block of each job): kernel rows
-// (2 M_cap - 1 blocks per job), columns (L_cap / 2 + 1) and data rows (M_cap); blocks beyond
+// (M_cap blocks per job), columns (L_cap / 2 + 1) and data rows (M_cap); blocks beyond
 // the job's current size return at once.  L_max: the largest capacity (shared memory).
 struct FftBatchJob {
     const ConvGeom *cg;
