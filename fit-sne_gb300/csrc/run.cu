@@ -5,8 +5,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <atomic>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fitsne_gb300.h"
@@ -629,9 +631,32 @@ int fitsne_batch_run(int njobs, const double *const *X, const int *N, const int 
             }
         } free_p{Ps};
         std::vector<const double *> Y0(njobs);
+        // similarities of the jobs on a few host threads, each with its own stream, so that
+        // the small jobs' kernels share the GPU
+        {
+            std::vector<int> rcs(njobs, 0);
+            std::vector<std::string> msgs(njobs);
+            std::atomic<int> next{0};
+            int dev = 0;
+            cudaGetDevice(&dev);
+            auto worker = [&]() {
+                cudaSetDevice(dev);
+                Stream ws;
+                for (int j = next++; j < njobs; j = next++) {
+                    rcs[j] = build_P(X[j], N[j], D[j], perplexity[j], -1, -1.0, 0, nullptr, &Ps[j], ws.s, false, false);
+                    if (rcs[j]) msgs[j] = fitsne_last_error();
+                }
+            };
+            const int nt = std::min(njobs, 8);
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+            worker();
+            for (auto &t : pool) t.join();
+            for (int j = 0; j < njobs; ++j)
+                if (rcs[j]) return set_error(rcs[j], msgs[j]);
+            if (cudaDeviceSynchronize() != cudaSuccess) return set_error(FITSNE_E_CUDA, "similarity stage failed");
+        }
         for (int j = 0; j < njobs; ++j) {
-            rc = build_P(X[j], N[j], D[j], perplexity[j], -1, -1.0, 0, nullptr, &Ps[j], st.s, false, false);
-            if (rc) return rc;
             if (!skip_random_init) {
                 std::srand(rand_seed ? (unsigned int) rand_seed[j] : 0u);
                 for (size_t i = 0; i < (size_t) N[j] * no_dims; ++i) Y[j][i] = randn_polar() * .0001;
