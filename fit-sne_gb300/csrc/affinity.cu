@@ -273,6 +273,142 @@ __global__ void k_sym_rows(const uint32_t *__restrict__ row, const uint32_t *__r
 }
 
 // ---------------------------------------------------------------------------------
+// Warp-per-row forms of k_row_sorted and k_sym_rows for rows of at most kWarpRow entries (the
+// kNN rows: K per row; longer rows keep the thread-per-row kernels above).  Same outputs,
+// entry for entry: the sort is by column (columns of a row are distinct), and each group of
+// an output row is compacted in its own order with warp ballots.
+constexpr int kWarpRow = 256;
+
+__global__ void __launch_bounds__(128) k_row_sorted_warp(const uint32_t *__restrict__ row,
+                                                         const uint32_t *__restrict__ col, int N,
+                                                         uint32_t *__restrict__ scol, uint32_t *__restrict__ spos,
+                                                         int *__restrict__ long_rows) {
+    __shared__ unsigned long long buf[4][kWarpRow];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned long long *b = buf[w];
+    for (int r = blockIdx.x * 4 + w; r < N; r += gridDim.x * 4) {
+        const uint32_t a = row[r], len = row[r + 1] - a;
+        if (len > (uint32_t) kWarpRow) {  // left to the thread-per-row kernel
+            if (lane == 0) atomicOr(long_rows, 1);
+            continue;
+        }
+        int n = 32;
+        while (n < (int) len) n <<= 1;
+        for (int i = lane; i < n; i += 32)
+            b[i] = i < (int) len ? ((unsigned long long) col[a + i] << 32) | (unsigned long long) (a + i) : ~0ull;
+        __syncwarp();
+        for (int k = 2; k <= n; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < n; i += 32) {
+                    const int q = i ^ j;
+                    if (q > i) {
+                        const unsigned long long x = b[i], y = b[q];
+                        if ((x > y) == ((i & k) == 0)) {
+                            b[i] = y;
+                            b[q] = x;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int i = lane; i < (int) len; i += 32) {
+            scol[a + i] = (uint32_t) (b[i] >> 32);
+            spos[a + i] = (uint32_t) b[i];
+        }
+        __syncwarp();
+    }
+}
+
+// One warp per output row; rows with more than kWarpRow entries or incoming edges are left to
+// k_sym_rows (long_rows set).
+template <bool FILL>
+__global__ void __launch_bounds__(128) k_sym_rows_warp(const uint32_t *__restrict__ row,
+                                                       const uint32_t *__restrict__ col,
+                                                       const double *__restrict__ val,
+                                                       const uint32_t *__restrict__ scol,
+                                                       const uint32_t *__restrict__ spos,
+                                                       const uint32_t *__restrict__ toff,
+                                                       const uint32_t *__restrict__ tedge,
+                                                       const uint32_t *__restrict__ src, int N,
+                                                       uint32_t *__restrict__ count, const uint32_t *__restrict__ srow,
+                                                       uint32_t *__restrict__ ocol, double *__restrict__ oval,
+                                                       int *__restrict__ long_rows) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int r = gw; r < N; r += nw) {
+        const uint32_t ur = (uint32_t) r;
+        const uint32_t r0 = row[r], r1 = row[r + 1], t0 = toff[r], t1 = toff[r + 1];
+        if (r1 - r0 > (uint32_t) kWarpRow || t1 - t0 > (uint32_t) kWarpRow) {
+            if (lane == 0) atomicOr(long_rows, 1);
+            continue;
+        }
+        uint32_t o = FILL ? srow[r] : 0u;
+        uint32_t c0 = 0;
+        const uint32_t lanemask = (1u << lane) - 1u;
+        // first group: incoming n < r, in incoming order (ascending n)
+        for (uint32_t base = t0; base < t1; base += 32) {
+            const uint32_t t = base + lane;
+            bool keep = false;
+            uint32_t n = 0, e = 0;
+            if (t < t1) {
+                e = tedge[t];
+                n = src[e];
+                keep = n < ur;
+            }
+            const unsigned m = __ballot_sync(full, keep);
+            if (FILL && keep) {
+                const uint32_t at = o + __popc(m & lanemask);
+                const uint32_t mm = find_in_row(row, scol, spos, ur, n);
+                ocol[at] = n;
+                oval[at] = (mm != 0xffffffffu) ? (val[e] + val[mm]) / 2.0 : val[e] / 2.0;
+            }
+            o += __popc(m);
+            c0 += __popc(m);
+        }
+        // middle: own entries in list order, except those mirrored earlier
+        for (uint32_t base = r0; base < r1; base += 32) {
+            const uint32_t e = base + lane;
+            bool keep = false;
+            uint32_t c = 0, mm = 0xffffffffu;
+            if (e < r1) {
+                c = col[e];
+                mm = find_in_row(row, scol, spos, c, ur);
+                keep = !(mm != 0xffffffffu && c < ur);
+            }
+            const unsigned m = __ballot_sync(full, keep);
+            if (FILL && keep) {
+                const uint32_t at = o + __popc(m & lanemask);
+                ocol[at] = c;
+                oval[at] = (mm != 0xffffffffu) ? (val[e] + val[mm]) / 2.0 : val[e] / 2.0;
+            }
+            o += __popc(m);
+            c0 += __popc(m);
+        }
+        // last group: incoming n > r that r does not list, in incoming order
+        for (uint32_t base = t0; base < t1; base += 32) {
+            const uint32_t t = base + lane;
+            bool keep = false;
+            uint32_t n = 0, e = 0;
+            if (t < t1) {
+                e = tedge[t];
+                n = src[e];
+                keep = n > ur && find_in_row(row, scol, spos, ur, n) == 0xffffffffu;
+            }
+            const unsigned m = __ballot_sync(full, keep);
+            if (FILL && keep) {
+                const uint32_t at = o + __popc(m & lanemask);
+                ocol[at] = n;
+                oval[at] = val[e] / 2.0;
+            }
+            o += __popc(m);
+            c0 += __popc(m);
+        }
+        if (!FILL && lane == 0) count[r] = c0;
+    }
+}
+
+// ---------------------------------------------------------------------------------
 __global__ void k_sum_part(const double *__restrict__ v, size_t n, double *__restrict__ part) {
     __shared__ double sh[32];
     double s = 0.0;
@@ -463,6 +599,7 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     const size_t nnz = in.nnz;
     uint32_t *src = nullptr, *scol = nullptr, *spos = nullptr, *keys = nullptr, *tedge = nullptr, *kalt = nullptr,
              *valt = nullptr, *indeg = nullptr, *toff = nullptr, *cnt = nullptr;
+    int *long_rows = nullptr;
     void *scratch = nullptr;
     const size_t nz = nnz ? nnz : 1;
     ACK(cudaMalloc(&src, sizeof(uint32_t) * nz));
@@ -475,11 +612,18 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     ACK(cudaMalloc(&indeg, sizeof(uint32_t) * (N + 1)));
     ACK(cudaMalloc(&toff, sizeof(uint32_t) * (N + 2)));
     ACK(cudaMalloc(&cnt, sizeof(uint32_t) * (N + 1)));
+    ACK(cudaMalloc(&long_rows, sizeof(int) * 2));
     const size_t scr = radix_sort_scratch_bytes(nz) + scan_scratch_bytes((size_t) N + 1);
     ACK(cudaMalloc(&scratch, scr));
     const int g = 2048;
     k_row_src<<<(N + 255) / 256, 256, 0, st>>>(in.row, N, src);
-    k_row_sorted<<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, N, scol, spos);
+    // rows sorted by a warp each; rows too long for it by a thread each
+    ACK(cudaMemsetAsync(long_rows, 0, sizeof(int) * 2, st));
+    k_row_sorted_warp<<<std::min((N + 3) / 4, 8192), 128, 0, st>>>(in.row, in.col, N, scol, spos, long_rows);
+    int hlong[2] = {0, 0};
+    ACK(cudaMemcpyAsync(hlong, long_rows, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    if (hlong[0]) k_row_sorted<<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, N, scol, spos);
     // transpose: group edge ids by column, stable in edge order
     ACK(cudaMemcpyAsync(keys, in.col, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToDevice, st));
     k_iota<<<g, 256, 0, st>>>(tedge, nnz);
@@ -487,8 +631,16 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     ACK(cudaMemsetAsync(indeg, 0, sizeof(uint32_t) * (N + 1), st));
     k_count_in<<<g, 256, 0, st>>>(in.col, nnz, indeg);
     ACK(exclusive_scan_u32(indeg, toff, (size_t) N, scratch, st));
-    k_sym_rows<false><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, cnt,
-                                                       nullptr, nullptr, nullptr);
+    const int gw = std::min((N + 3) / 4, 8192);
+    k_sym_rows_warp<false><<<gw, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, cnt, nullptr,
+                                               nullptr, nullptr, long_rows + 1);
+    ACK(cudaMemcpyAsync(hlong + 1, long_rows + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ACK(cudaStreamSynchronize(st));
+    // rows with more than kWarpRow entries or incoming edges: the whole matrix by threads
+    const bool thread_rows = hlong[0] || hlong[1];
+    if (thread_rows)
+        k_sym_rows<false><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
+                                                           cnt, nullptr, nullptr, nullptr);
     DevCSR P;
     P.N = N;
     ACK(cudaMalloc(&P.row, sizeof(uint32_t) * (N + 1)));
@@ -499,8 +651,12 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     P.nnz = total;
     ACK(cudaMalloc(&P.col, sizeof(uint32_t) * (total ? total : 1)));
     ACK(cudaMalloc(&P.val, sizeof(double) * (total ? total : 1)));
-    k_sym_rows<true><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
-                                                      nullptr, P.row, P.col, P.val);
+    if (thread_rows)
+        k_sym_rows<true><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
+                                                          nullptr, P.row, P.col, P.val);
+    else
+        k_sym_rows_warp<true><<<gw, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, nullptr,
+                                                  P.row, P.col, P.val, long_rows + 1);
     ACK(cudaGetLastError());
     ACK(cudaStreamSynchronize(st));
     cudaFree(src);
@@ -513,6 +669,7 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     cudaFree(indeg);
     cudaFree(toff);
     cudaFree(cnt);
+    cudaFree(long_rows);
     cudaFree(scratch);
     *out = P;
     return 0;

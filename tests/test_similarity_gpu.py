@@ -107,16 +107,23 @@ def test_symmetrize_matches_reference_exactly(gpu_lib, golden):
     assert np.array_equal(v, golden["sym_val"])
 
 
-@pytest.mark.parametrize("N,kmax,seed", [(500, 9, 0), (20000, 30, 1)])
-def test_symmetrize_general_csr_matches_oracle(gpu_lib, orc, N, kmax, seed):
+@pytest.mark.parametrize("N,kmax,seed,hub", [(500, 9, 0, False), (20000, 30, 1, False), (3000, 20, 2, True)])
+def test_symmetrize_general_csr_matches_oracle(gpu_lib, orc, N, kmax, seed, hub):
+    """Entry-for-entry equality with the restated symmetrizeMatrix on random CSR patterns
+    (empty rows, self loops); "hub": one row lists 400 points and 300 rows list point 7, so that
+    rows longer than a warp's 256 entries take the thread-per-row kernels."""
     rng = np.random.default_rng(seed)
     lens = rng.integers(0, kmax + 1, N)
+    if hub:
+        lens[3] = 400
     row = np.concatenate([[0], np.cumsum(lens)]).astype(np.uint32)
     cols = []
     for i in range(N):
         c = rng.choice(N, lens[i], replace=False)
         if i % 97 == 0 and lens[i] > 0 and i not in c:
             c[0] = i  # self loops appear with duplicate points
+        if hub and 100 <= i < 400 and lens[i] > 0 and 7 not in c:
+            c[0] = 7  # many incoming edges of point 7
         cols.append(c)
     col = np.concatenate(cols).astype(np.uint32)
     val = rng.random(len(col))
