@@ -312,6 +312,10 @@ FITSNE_D void center_minmax_body(T *Y, int N, int apply_mean, int excl, RedScrat
             negm[d] = -m;
     }
     double mn = HUGE_VAL, mx = -HUGE_VAL;
+    // FP32 form: the double-float values compared by their (hi, lo) pairs, whose order is the
+    // values' order for normalised pairs (hi = fl(hi + lo)), so the thread's min / max cost one
+    // conversion to double at the end instead of FP64 operations per coordinate
+    float nh = INFINITY, nl = 0.f, xh = -INFINITY, xl = 0.f;
     for (int i = blk * blockDim.x + threadIdx.x; i < N; i += nblk * blockDim.x) {
         P c[D];
         YL<T, D>::load(Y, i, c);
@@ -322,12 +326,29 @@ FITSNE_D void center_minmax_body(T *Y, int N, int apply_mean, int excl, RedScrat
         }
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            const double v = ptod(c[d]);
-            mx = fmax(mx, v);
             // 2-D: the first coordinate of the first point never reaches the min
             // (if / else-if pair of tsne.cpp:1045-1048)
-            if (!(D == 2 && i == excl && d == 0)) mn = fmin(mn, v);
+            const bool in_min = !(D == 2 && i == excl && d == 0);
+            if constexpr (sizeof(T) == 4) {
+                const df32 v = c[d];
+                if (v.hi > xh || (v.hi == xh && v.lo > xl)) {
+                    xh = v.hi;
+                    xl = v.lo;
+                }
+                if (in_min && (v.hi < nh || (v.hi == nh && v.lo < nl))) {
+                    nh = v.hi;
+                    nl = v.lo;
+                }
+            } else {
+                const double v = ptod(c[d]);
+                mx = fmax(mx, v);
+                if (in_min) mn = fmin(mn, v);
+            }
         }
+    }
+    if constexpr (sizeof(T) == 4) {
+        mn = (double) nh + (double) nl;
+        mx = (double) xh + (double) xl;
     }
     if (grid_minmax<2>(mn, mx, r.part, r.count + 0, sh, blk, nblk)) {
         r.mnmx[0] = mn;

@@ -178,3 +178,18 @@ def test_batched_jobs_match_single_runs(gpu_lib, monkeypatch, mode):
         assert abs(costs[j][499] - c[499]) <= 1e-2 * c[499], j
         assert np.isfinite(Ys[j]).all()
     assert abs(costs[0][499] - g["df1"][499]) <= 1e-2 * g["df1"][499]
+
+
+def test_batched_one_dimensional_jobs(gpu_lib):
+    """1-D batches (outside the all-jobs pipeline: one graph per job) end where the jobs' own
+    runs end (final KL within 2 %: 800-point FP32 runs)."""
+    rng = np.random.default_rng(8)
+    Xs = [rng.standard_normal((800, 6)) + np.repeat(np.eye(6)[:4] * 5, 200, axis=0),
+          rng.standard_normal((600, 6)) + np.repeat(np.eye(6)[:3] * 5, 200, axis=0)]
+    Y0s = [rng.standard_normal((len(X), 1)) * 1e-4 for X in Xs]
+    lrs = [200.0, 200.0]
+    Ys, costs, st = gpu_lib.batch_run(Xs, [20.0, 20.0], learning_rates=lrs, Y0s=Y0s, no_dims=1, max_iter=300)
+    for j, X in enumerate(Xs):
+        _, c = gpu_lib.run(X, no_dims=1, Y0=Y0s[j], perplexity=20.0, learning_rate=lrs[j], max_iter=300)
+        assert Ys[j].shape == (len(X), 1) and np.isfinite(Ys[j]).all()
+        assert abs(costs[j][299] - c[299]) <= 2e-2 * c[299], j
