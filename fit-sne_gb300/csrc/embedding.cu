@@ -388,7 +388,7 @@ int Embedding<T>::step(const UpdateParams &p, bool) {
     }
     rc = repulsion();
     if (rc) return rc;
-    if (attr_shape_ < 0) {
+    if (attr_shape_ < 0 || (attr_placeholder_ && tune_ready_)) {
         rc = tune_attr(true);
         if (rc) return rc;
     }
@@ -492,6 +492,7 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
             int rr = reorder();
             if (rr) return rr;
         }
+        tune_ready_ = s.stop_lying_iter < 0 || it > s.stop_lying_iter;
         int rc = step(p, it == 0);
         if (rc) return rc;
         if (it == s.stop_lying_iter) mult /= s.early_exag_coeff;
@@ -537,10 +538,10 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
 // `measure` is set, the candidate shapes are timed on the attraction pass (gradient only: no
 // state changes) of this embedding's data and the fastest is kept.  Choices are shared by
 // embeddings of the same size class (type, dimension, log2 N, log2 nnz / N, renumbered or not)
-// within the process.  An embedding that will be renumbered for locality (run schedule, N >=
-// kReorderMinN) runs the default shape until its first renumbering and is timed after it, on
-// the numbering of the iterations that follow; one-off gradients (measure false) take the
-// cached choice or the default.
+// within the process.  The shapes are timed on a state like that of most iterations: after the
+// early exaggeration (the schedule sets tune_ready_) and after the first locality renumbering
+// (run schedule, N >= kReorderMinN); until then the default shape runs.  One-off gradients
+// (measure false) take the cached choice or the default.
 template <typename T>
 int Embedding<T>::tune_attr(bool measure) {
     // candidates, the default first: the shapes that came out ahead on some size class
@@ -569,10 +570,12 @@ int Embedding<T>::tune_attr(bool measure) {
         }
     }
     const bool renumber_ahead = !reordered_ && reorder_enabled_ && N_ >= kReorderMinN;
-    if (!measure || renumber_ahead) {
+    if (!measure || renumber_ahead || !tune_ready_) {
         attr_shape_ = kCandidates[0];  // not cached: a later call may measure
+        attr_placeholder_ = true;
         return 0;
     }
+    attr_placeholder_ = false;
     const char *e = std::getenv("FITSNE_AUTOTUNE");
     int best = kCandidates[0];
     if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
@@ -622,7 +625,7 @@ int Embedding<T>::tune_attr(bool measure) {
 
 template <typename T>
 int Embedding<T>::plan_capacity(int grow) {
-    if (attr_shape_ < 0) {
+    if (attr_shape_ < 0 || (attr_placeholder_ && tune_ready_)) {
         int tr = tune_attr(true);
         if (tr) return tr;
     }
@@ -891,6 +894,8 @@ int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, doubl
             ++end;
         const int len = end - it;
         const UpdateParams p = params(it);
+        // launch shapes are timed on the state of the iterations after the early exaggeration
+        tune_ready_ = s.stop_lying_iter < 0 || it > s.stop_lying_iter;
         int grow = 0;
         while (true) {
             auto t = clk::now();

@@ -174,6 +174,8 @@ class Embedding {
     // autotuned launch shape of the attraction pass (-1: not chosen yet); re-chosen after a
     // locality renumbering, since the gathers' locality decides between the shapes
     int attr_shape_ = -1;
+    bool attr_placeholder_ = false;  // attr_shape_ is the default, to be measured when tune_ready_
+    bool tune_ready_ = true;         // the run is past its early exaggeration
     int tune_attr(bool measure);
     // graph chunks
     bool graphs_ = true;
