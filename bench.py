@@ -191,9 +191,10 @@ def bf16_peak():
 
 
 # DRAM bytes (read + write) of one attraction launch / its algorithmic bytes, from an ncu
-# capture of k_attr at N = 200,000 (nnz = 30,344,422): 256,773,632 / 257,955,380.  Traffic
-# grows with nnz (the CSR stream dominates), so the ratio carries to N = 1M.
-ATTR_TRAFFIC_RATIO = 256773632 / 257955380
+# capture of k_attr on this workload (N = 1,000,000, nnz = 155,720,438; the 301st launch):
+# 1,355,542,000 + 28,894,976 bytes against 1,321,763,508 algorithmic.  (At N = 200,000 the
+# ratio was 0.995: 256,773,632 / 257,955,380.)
+ATTR_TRAFFIC_RATIO = (1355542000 + 28894976) / 1321763508
 
 
 def attraction_bytes(N, nnz):

@@ -411,13 +411,27 @@ __global__ void __launch_bounds__(kBlock) k_spread(const T *__restrict__ Y, int 
 
 // FP32 spread with nterms = 3, aggregated per warp before the atomics.  After the locality
 // renumbering consecutive points mostly share a box, and every point of a box charges the
-// same 9 (2-D) or 3 (1-D) nodes: a segmented inclusive scan over runs of equal box index
-// (head flags where the box changes, five shuffle steps per charge value) leaves each run's
-// sums in its last lane, which alone issues the node atomics.  Identical charges to
-// k_spread; only the order of the FP32 additions differs.
+// same 9 (2-D) or 3 (1-D) nodes, so a warp sums its 32 points' charges over runs of equal box
+// index and issues one atomic per run and node.  2-D: the 36 values per point go through a
+// per-warp shared-memory table (9 stores per lane, then 32 loads by each of 9 node lanes)
+// instead of a segmented shuffle scan (180 shuffles per warp).  1-D (9 values): a segmented
+// inclusive scan (head flags where the box changes, five shuffle steps per value) leaves each
+// run's sums in its last lane.  Identical charges to k_spread; only the order of the FP32
+// additions differs.
+struct SpreadWarpTable {
+    float4 v[9][33];      // [node][point]; 33 columns so that the node lanes' loads spread over banks
+    long long cell[32];   // first grid cell of each point's box (-1: no point)
+};
+constexpr int kSpreadWarps = kBlock / 32;
+
 template <int D>
 FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<float> &b,
                                Cell4<float> *__restrict__ grid, int blk, int nblk) {
+    SpreadWarpTable *wb = nullptr;
+    if constexpr (D == 2) {
+        __shared__ SpreadWarpTable tables[kSpreadWarps];
+        wb = &tables[threadIdx.x >> 5];
+    }
     constexpr int NT = 3;
     constexpr int NV = (D == 2) ? NT * NT : NT;  // nodes per point
     constexpr int NC = (D == 2) ? 4 : 3;         // charge values per node
@@ -474,35 +488,52 @@ FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<fl
                 v[ia][2] = ww * u * u;
             }
         }
-        // segmented inclusive scan: after the step with offset `off`, lane l holds the sum
-        // over [max(head(l), l - 2 off + 1), l]
-        const int prev = __shfl_up_sync(full, key, 1);
-        const unsigned heads = __ballot_sync(full, lane == 0 || prev != key);
-        const int my_head = 31 - __clz(heads & (full >> (31 - lane)));
+        if constexpr (D == 2) {
+            // run sums through the warp's table: lane l stores its 9 node charges in column l;
+            // lane q < 9 then adds up row q (node q) in point order and, at the end of each run,
+            // issues that node's float4 atomic for the run's box
+            const int next = __shfl_down_sync(full, key, 1);
+            const unsigned ends = __ballot_sync(full, lane == 31 || next != key);
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const bool take = lane - off >= my_head;
-#pragma unroll
-            for (int q = 0; q < NV; ++q)
-#pragma unroll
-                for (int r = 0; r < NC; ++r) {
-                    const float y = __shfl_up_sync(full, v[q][r], off);
-                    if (take) v[q][r] += y;
-                }
-        }
-        const int next = __shfl_down_sync(full, key, 1);
-        if (valid && (lane == 31 || next != key)) {
-            if constexpr (D == 2) {
-#pragma unroll
-                for (int ia = 0; ia < NT; ++ia) {
-                    const size_t rowbase = (size_t) (bx[0] * NT + ia) * b.M + bx[1] * NT;
-#pragma unroll
-                    for (int ib = 0; ib < NT; ++ib) {
-                        const float *o = v[ia * NT + ib];
-                        atomicAdd(reinterpret_cast<float4 *>(grid + rowbase + ib), make_float4(o[0], o[1], o[2], o[3]));
+            for (int q = 0; q < NV; ++q) wb->v[q][lane] = make_float4(v[q][0], v[q][1], v[q][2], v[q][3]);
+            wb->cell[lane] = valid ? (long long) bx[0] * NT * b.M + (long long) bx[1] * NT : -1ll;
+            __syncwarp();
+            if (lane < NV) {
+                const long long off = (long long) (lane / NT) * b.M + lane % NT;
+                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int pt = 0; pt < 32; ++pt) {
+                    const float4 x = wb->v[lane][pt];
+                    acc.x += x.x;
+                    acc.y += x.y;
+                    acc.z += x.z;
+                    acc.w += x.w;
+                    if ((ends >> pt) & 1u) {
+                        const long long c = wb->cell[pt];
+                        if (c >= 0) atomicAdd(reinterpret_cast<float4 *>(grid + c + off), acc);
+                        acc = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
                 }
-            } else {
+            }
+            __syncwarp();  // the table is rewritten by the next 32 points
+        } else {
+            // segmented inclusive scan: after the step with offset `off`, lane l holds the sum
+            // over [max(head(l), l - 2 off + 1), l]
+            const int prev = __shfl_up_sync(full, key, 1);
+            const unsigned heads = __ballot_sync(full, lane == 0 || prev != key);
+            const int my_head = 31 - __clz(heads & (full >> (31 - lane)));
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const bool take = lane - off >= my_head;
+#pragma unroll
+                for (int q = 0; q < NV; ++q)
+#pragma unroll
+                    for (int r = 0; r < NC; ++r) {
+                        const float y = __shfl_up_sync(full, v[q][r], off);
+                        if (take) v[q][r] += y;
+                    }
+            }
+            const int next = __shfl_down_sync(full, key, 1);
+            if (valid && (lane == 31 || next != key)) {
 #pragma unroll
                 for (int ia = 0; ia < NT; ++ia) {
                     float *cell = reinterpret_cast<float *>(grid + bx[0] * NT + ia);
