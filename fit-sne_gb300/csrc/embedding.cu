@@ -492,7 +492,7 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
             int rr = reorder();
             if (rr) return rr;
         }
-        tune_ready_ = s.stop_lying_iter < 0 || it > s.stop_lying_iter;
+        tune_ready_ = tune_state(s, it);
         int rc = step(p, it == 0);
         if (rc) return rc;
         if (it == s.stop_lying_iter) mult /= s.early_exag_coeff;
@@ -535,19 +535,22 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
 // (k_geometry) inside a capacity chosen here; the host reads the status once per chunk.
 //
 // Chooses the attraction pass's launch shape: FITSNE_ATTR_SHAPE fixes it; otherwise, when
-// `measure` is set, the candidate shapes are timed on the attraction pass (gradient only: no
-// state changes) of this embedding's data and the fastest is kept.  Choices are shared by
+// `measure` is set, the candidate shapes are timed on the attraction pass with the optimiser
+// step of this embedding's data (on scratch copies of the state) and the fastest is kept.  Choices are shared by
 // embeddings of the same size class (type, dimension, log2 N, log2 nnz / N, renumbered or not)
-// within the process.  The shapes are timed on a state like that of most iterations: after the
-// early exaggeration (the schedule sets tune_ready_) and after the first locality renumbering
-// (run schedule, N >= kReorderMinN); until then the default shape runs.  One-off gradients
-// (measure false) take the cached choice or the default.
+// within the process.  The shapes are timed on a state like that of the later iterations
+// (tune_state: after the early exaggeration and after the last locality renumbering); until
+// then the default shape runs.  One-off gradients (measure false) take the cached choice or the
+// default.
 template <typename T>
 int Embedding<T>::tune_attr(bool measure) {
     // candidates, the default first: the shapes that came out ahead on some size class
-    // (grad.cu describes them); 16 rows x 2 edges per lane was the fastest at N = 1M
-    static const int kCandidates[] = {3, 0, 2, 9};
-    constexpr int kNumCandidates = (int) (sizeof(kCandidates) / sizeof(kCandidates[0]));
+    // (grad.cu describes them).  FP32: 16 rows x 2 edges per lane with 48 warps per SM was the
+    // fastest at N = 1M; FP64 (twice the registers per value): 16 x 2 with 32 warps.
+    static const int kCandidates32[] = {10, 3, 0, 2, 9};
+    static const int kCandidates64[] = {3, 0, 2, 9};
+    const int *kCandidates = sizeof(T) == 4 ? kCandidates32 : kCandidates64;
+    const int kNumCandidates = sizeof(T) == 4 ? 5 : 4;
     static std::mutex mu;
     static std::map<std::vector<int>, int> chosen;
     int lgN = 0, lgK = 0;
@@ -579,26 +582,41 @@ int Embedding<T>::tune_attr(bool measure) {
     const char *e = std::getenv("FITSNE_AUTOTUNE");
     int best = kCandidates[0];
     if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
+        // the launches time the optimiser step itself (mode 1, the kernel the iterations run):
+        // the new Y goes to the free buffer, the gains and momentum to copies, and the pending
+        // mean of Y (written by the step's reduction) is kept aside and put back afterwards
         UpdateParams p{};
-        p.mode = 0;
+        p.mode = 1;
+        p.use_gains = 1;
         p.exag = 1.0;
+        p.momentum = 0.8;
+        p.learning_rate = 200.0;
+        p.max_step_norm = 5.0;
         p.df = gp_.df;
+        const size_t nd = (size_t) N_ * D_;
+        T *scr = nullptr;
+        FITSNE_CK(cudaMalloc(&scr, sizeof(T) * 2 * nd));
+        FITSNE_CK(cudaMemcpyAsync(scr, uY_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+        FITSNE_CK(cudaMemcpyAsync(scr + nd, gains_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+        double *mean_keep = red_.mnmx + 8;
+        FITSNE_CK(cudaMemcpyAsync(mean_keep, red_.mean, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st_));
         cudaEvent_t a = nullptr, b = nullptr;
         FITSNE_CK(cudaEventCreate(&a));
         FITSNE_CK(cudaEventCreate(&b));
         float best_ms = 0.f;
         for (int ci = 0; ci < kNumCandidates; ++ci) {
             const int sh = kCandidates[ci];
-            FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_,
-                                            p, red_, st_, sh, yh_));
+            FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr, rep_,
+                                            N_, D_, p, red_, st_, sh, yh_));
             FITSNE_CK(cudaEventRecord(a, st_));
             for (int r = 0; r < 3; ++r)
-                FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_,
-                                                D_, p, red_, st_, sh, yh_));
+                FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr,
+                                                rep_, N_, D_, p, red_, st_, sh, yh_));
             FITSNE_CK(cudaEventRecord(b, st_));
             FITSNE_CK(cudaEventSynchronize(b));
             float ms = 0.f;
             cudaEventElapsedTime(&ms, a, b);
+            if (timing_requested()) std::fprintf(stderr, "[fitsne] attraction shape %d: %.4f ms\n", sh, ms / 3.f);
             // another shape must beat the best so far by 3 % (timing noise)
             if (ci == 0 || ms < 0.97f * best_ms) {
                 best = sh;
@@ -608,6 +626,9 @@ int Embedding<T>::tune_attr(bool measure) {
         launches_ += 4 * kNumCandidates;
         cudaEventDestroy(a);
         cudaEventDestroy(b);
+        FITSNE_CK(cudaMemcpyAsync(red_.mean, mean_keep, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st_));
+        FITSNE_CK(cudaStreamSynchronize(st_));
+        FITSNE_CK(cudaFree(scr));
         if (timing_requested()) {
             int g = 0, u = 0;
             attr_shape_info(best, &g, &u);
@@ -700,7 +721,7 @@ int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_f
             FITSNE_CK(conv1d_launch_dev<T>(grid_in_, grid_out_, L_cap_, cg, tw_dev_, work_a_, gp_.df, mode, st_));
         FITSNE_CK(launch_gather_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_out_, mode, rep_, red_, st_, yh_));
         FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[c], Y_[1 - c], uY_, gains_, nullptr, rep_, N_, D_, p,
-                                        red_, st_, attr_shape_ < 0 ? 0 : attr_shape_, yh_));
+                                        red_, st_, attr_shape_ < 0 ? (sizeof(T) == 4 ? 10 : 3) : attr_shape_, yh_));
         c = 1 - c;
     }
     FITSNE_CK(cudaMemcpyAsync(h_gstat_, gstatus_, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -894,8 +915,8 @@ int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, doubl
             ++end;
         const int len = end - it;
         const UpdateParams p = params(it);
-        // launch shapes are timed on the state of the iterations after the early exaggeration
-        tune_ready_ = s.stop_lying_iter < 0 || it > s.stop_lying_iter;
+        // launch shapes are timed on the state of the later iterations
+        tune_ready_ = tune_state(s, it);
         int grow = 0;
         while (true) {
             auto t = clk::now();

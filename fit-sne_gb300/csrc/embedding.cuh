@@ -114,6 +114,15 @@ class Embedding {
                (it == 50 || it == 150 || it == 300 || it == 600 || (!reordered_ && it == it0 && it0 > 50));
     }
     int reorder_now() { return reorder(); }
+    // Whether iteration it is in the state the attraction's launch shapes are timed on: past
+    // the early exaggeration, and, when the embedding is renumbered, past the last renumbering
+    // (iteration 600).  Right after the exaggeration the embedding still expands fast and its
+    // attraction (about 1 ms at N = 1M instead of 0.7) ranks the shapes differently.
+    bool tune_state(const Schedule &s, int it) const {
+        const bool exag_done = s.stop_lying_iter < 0 || it > s.stop_lying_iter;
+        const bool renumbers = reorder_enabled_ && N_ >= kReorderMinN;
+        return exag_done && (!renumbers || it >= 600);
+    }
     const StageTimes &last_times() const { return times_; }
     const GridGeom &last_geom() const { return geom_; }
     int last_L() const { return L_; }

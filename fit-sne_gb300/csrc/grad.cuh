@@ -163,7 +163,7 @@ cudaError_t launch_geometry(RedScratch r, int D, int nterms, double ipi, int min
                             DevGeom *dg, int *status_acc, cudaStream_t st);
 // Number of attraction launch shapes (rows per work item x edges per lane; see grad.cu) and
 // the shape of an index.
-constexpr int kNumAttrShapes = 10;
+constexpr int kNumAttrShapes = 11;
 int attr_shape_info(int shape, int *group, int *unroll);
 // yh (FP32 form only, may be null): the FP32 positions k_gather wrote for this Y, which the
 // attraction then gathers as its neighbours' positions (8 instead of 16 bytes per point in

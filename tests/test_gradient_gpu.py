@@ -104,7 +104,7 @@ def test_fp32_box_index_agrees_with_fp64_on_a_box_edge(gpu_lib, golden):
     assert rel_l2(g32, g64) < 1e-5
 
 
-N_SHAPES = 10  # attraction launch shapes (kNumAttrShapes)
+N_SHAPES = 11  # attraction launch shapes (kNumAttrShapes)
 
 
 @pytest.mark.parametrize("shape", range(N_SHAPES))
