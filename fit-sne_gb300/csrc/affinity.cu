@@ -172,10 +172,14 @@ __global__ void k_row_src(const uint32_t *__restrict__ row, int N, uint32_t *__r
 }
 
 // per-row copy of (col, position) sorted by col (insertion sort; rows are short)
+// Rows longer than kWarpRow entries (the warp-per-row kernels below take the others).
+constexpr int kWarpRow = 256;
+
 __global__ void k_row_sorted(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col, int N,
                              uint32_t *__restrict__ scol, uint32_t *__restrict__ spos) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
         const uint32_t a = row[r], b = row[r + 1];
+        if (b - a <= (uint32_t) kWarpRow) continue;
         for (uint32_t e = a; e < b; ++e) {
             const uint32_t c = col[e];
             uint32_t k = e;
@@ -219,6 +223,8 @@ __global__ void k_count_in(const uint32_t *__restrict__ col, size_t nnz, uint32_
 
 // Output row r: incoming n < r (ascending), r's own entries in list order except those
 // mirrored earlier, incoming n > r that r does not list (ascending)  (tsne.cpp:1772-1811).
+// Only the rows with more than kWarpRow entries or incoming edges (the warp-per-row kernel
+// below takes the others).
 template <bool FILL>
 __global__ void k_sym_rows(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
                            const double *__restrict__ val, const uint32_t *__restrict__ scol,
@@ -227,6 +233,7 @@ __global__ void k_sym_rows(const uint32_t *__restrict__ row, const uint32_t *__r
                            uint32_t *__restrict__ count, const uint32_t *__restrict__ srow,
                            uint32_t *__restrict__ ocol, double *__restrict__ oval) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
+        if (row[r + 1] - row[r] <= (uint32_t) kWarpRow && toff[r + 1] - toff[r] <= (uint32_t) kWarpRow) continue;
         uint32_t o = FILL ? srow[r] : 0u;
         uint32_t c0 = 0;
         const uint32_t ur = (uint32_t) r;
@@ -277,7 +284,6 @@ __global__ void k_sym_rows(const uint32_t *__restrict__ row, const uint32_t *__r
 // kNN rows: K per row; longer rows keep the thread-per-row kernels above).  Same outputs,
 // entry for entry: the sort is by column (columns of a row are distinct), and each group of
 // an output row is compacted in its own order with warp ballots.
-constexpr int kWarpRow = 256;
 
 __global__ void __launch_bounds__(128) k_row_sorted_warp(const uint32_t *__restrict__ row,
                                                          const uint32_t *__restrict__ col, int N,
@@ -636,7 +642,7 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
                                                nullptr, nullptr, long_rows + 1);
     ACK(cudaMemcpyAsync(hlong + 1, long_rows + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     ACK(cudaStreamSynchronize(st));
-    // rows with more than kWarpRow entries or incoming edges: the whole matrix by threads
+    // rows with more than kWarpRow entries or incoming edges: a thread each
     const bool thread_rows = hlong[0] || hlong[1];
     if (thread_rows)
         k_sym_rows<false><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
@@ -651,12 +657,11 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     P.nnz = total;
     ACK(cudaMalloc(&P.col, sizeof(uint32_t) * (total ? total : 1)));
     ACK(cudaMalloc(&P.val, sizeof(double) * (total ? total : 1)));
+    k_sym_rows_warp<true><<<gw, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, nullptr,
+                                              P.row, P.col, P.val, long_rows + 1);
     if (thread_rows)
         k_sym_rows<true><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
                                                           nullptr, P.row, P.col, P.val);
-    else
-        k_sym_rows_warp<true><<<gw, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, nullptr,
-                                                  P.row, P.col, P.val, long_rows + 1);
     ACK(cudaGetLastError());
     ACK(cudaStreamSynchronize(st));
     cudaFree(src);
