@@ -388,7 +388,7 @@ int Embedding<T>::step(const UpdateParams &p, bool) {
     }
     rc = repulsion();
     if (rc) return rc;
-    if (attr_shape_ < 0 || (attr_placeholder_ && tune_ready_)) {
+    if (attr_shape_ < 0 || attr_phase_ != tune_phase_) {
         rc = tune_attr(true);
         if (rc) return rc;
     }
@@ -492,7 +492,7 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
             int rr = reorder();
             if (rr) return rr;
         }
-        tune_ready_ = tune_state(s, it);
+        tune_phase_ = tune_phase(s, it);
         int rc = step(p, it == 0);
         if (rc) return rc;
         if (it == s.stop_lying_iter) mult /= s.early_exag_coeff;
@@ -536,28 +536,30 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
 //
 // Chooses the attraction pass's launch shape: FITSNE_ATTR_SHAPE fixes it; otherwise, when
 // `measure` is set, the candidate shapes are timed on the attraction pass with the optimiser
-// step of this embedding's data (on scratch copies of the state) and the fastest is kept.  Choices are shared by
-// embeddings of the same size class (type, dimension, log2 N, log2 nnz / N, renumbered or not)
-// within the process.  The shapes are timed on a state like that of the later iterations
-// (tune_state: after the early exaggeration and after the last locality renumbering); until
-// then the default shape runs.  One-off gradients (measure false) take the cached choice or the
+// step of this embedding's data (on scratch copies of the state) and the fastest is kept.
+// Choices are made per phase of the run (tune_phase: compact or expanded embedding) and shared
+// by embeddings of the same size class (type, dimension, log2 N, log2 nnz / N, renumbered or
+// not, phase) within the process.  An embedding that will be renumbered runs the default shape
+// until its first renumbering.  One-off gradients (measure false) take the cached choice or the
 // default.
 template <typename T>
 int Embedding<T>::tune_attr(bool measure) {
-    // candidates, the default first: the shapes that came out ahead on some size class
-    // (grad.cu describes them).  FP32: 16 rows x 2 edges per lane with 48 warps per SM was the
-    // fastest at N = 1M; FP64 (twice the registers per value): 16 x 2 with 32 warps.
-    static const int kCandidates32[] = {10, 3, 0, 2, 9};
-    static const int kCandidates64[] = {3, 0, 2, 9};
+    // candidates, the default first: the shapes that came out ahead on some size class and
+    // phase (grad.cu describes them).  FP32 at N = 1M: 16 rows x 2 edges per lane with 48
+    // warps per SM on the expanded embedding, 8 x 4 on the compact one; FP64 (twice the
+    // registers per value): 16 x 2 and 8 x 4 with 32 warps.
+    static const int kCandidates32[] = {10, 2, 3, 0};
+    static const int kCandidates64[] = {3, 2};
     const int *kCandidates = sizeof(T) == 4 ? kCandidates32 : kCandidates64;
-    const int kNumCandidates = sizeof(T) == 4 ? 5 : 4;
+    const int kNumCandidates = sizeof(T) == 4 ? 4 : 2;
     static std::mutex mu;
     static std::map<std::vector<int>, int> chosen;
     int lgN = 0, lgK = 0;
     while ((1 << (lgN + 1)) <= N_) ++lgN;
     const size_t per = N_ ? nnz_ / (size_t) N_ : 0;
     while (((size_t) 1 << (lgK + 1)) <= per) ++lgK;
-    const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0};
+    const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0, tune_phase_};
+    attr_phase_ = tune_phase_;
     const char *fixed = std::getenv("FITSNE_ATTR_SHAPE");  // a fixed shape index: no tuning, no cache
     if (fixed && *fixed) {
         const int sh = std::atoi(fixed);
@@ -573,12 +575,10 @@ int Embedding<T>::tune_attr(bool measure) {
         }
     }
     const bool renumber_ahead = !reordered_ && reorder_enabled_ && N_ >= kReorderMinN;
-    if (!measure || renumber_ahead || !tune_ready_) {
+    if (!measure || renumber_ahead) {
         attr_shape_ = kCandidates[0];  // not cached: a later call may measure
-        attr_placeholder_ = true;
         return 0;
     }
-    attr_placeholder_ = false;
     const char *e = std::getenv("FITSNE_AUTOTUNE");
     int best = kCandidates[0];
     if (!(e && std::atoi(e) == 0) && N_ >= 4096) {
@@ -609,21 +609,21 @@ int Embedding<T>::tune_attr(bool measure) {
             FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr, rep_,
                                             N_, D_, p, red_, st_, sh, yh_));
             FITSNE_CK(cudaEventRecord(a, st_));
-            for (int r = 0; r < 3; ++r)
+            for (int r = 0; r < 2; ++r)
                 FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr,
                                                 rep_, N_, D_, p, red_, st_, sh, yh_));
             FITSNE_CK(cudaEventRecord(b, st_));
             FITSNE_CK(cudaEventSynchronize(b));
             float ms = 0.f;
             cudaEventElapsedTime(&ms, a, b);
-            if (timing_requested()) std::fprintf(stderr, "[fitsne] attraction shape %d: %.4f ms\n", sh, ms / 3.f);
+            if (timing_requested()) std::fprintf(stderr, "[fitsne] attraction shape %d: %.4f ms\n", sh, ms / 2.f);
             // another shape must beat the best so far by 3 % (timing noise)
             if (ci == 0 || ms < 0.97f * best_ms) {
                 best = sh;
                 best_ms = ms;
             }
         }
-        launches_ += 4 * kNumCandidates;
+        launches_ += 3 * kNumCandidates;
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         FITSNE_CK(cudaMemcpyAsync(red_.mean, mean_keep, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st_));
@@ -632,8 +632,9 @@ int Embedding<T>::tune_attr(bool measure) {
         if (timing_requested()) {
             int g = 0, u = 0;
             attr_shape_info(best, &g, &u);
-            std::fprintf(stderr, "[fitsne] attraction launch shape %d (N=%d, nnz=%zu%s): %d rows per work item, %d "
-                                 "edges per lane\n", best, N_, nnz_, reordered_ ? ", renumbered" : "", g, u);
+            std::fprintf(stderr, "[fitsne] attraction launch shape %d (N=%d, nnz=%zu%s, phase %d): %d rows per work "
+                                 "item, %d edges per lane\n", best, N_, nnz_, reordered_ ? ", renumbered" : "",
+                         tune_phase_, g, u);
         }
     }
     {
@@ -646,7 +647,7 @@ int Embedding<T>::tune_attr(bool measure) {
 
 template <typename T>
 int Embedding<T>::plan_capacity(int grow) {
-    if (attr_shape_ < 0 || (attr_placeholder_ && tune_ready_)) {
+    if (attr_shape_ < 0 || attr_phase_ != tune_phase_) {
         int tr = tune_attr(true);
         if (tr) return tr;
     }
@@ -822,6 +823,7 @@ std::vector<unsigned long long> Embedding<T>::chunk_key(const UpdateParams &p, i
     put(&p.use_gains, sizeof p.use_gains);
     put(&nb_cap_, sizeof nb_cap_);
     put(&excl_, sizeof excl_);
+    put(&attr_shape_, sizeof attr_shape_);
     for (const void *q : {(const void *) row_, (const void *) col_, (const void *) val_, (const void *) Y_[0],
                           (const void *) Y_[1], (const void *) uY_, (const void *) gains_, (const void *) rep_,
                           (const void *) grid_in_, (const void *) grid_out_, (const void *) work_a_,
@@ -915,8 +917,8 @@ int Embedding<T>::run_schedule_graphs(const Schedule &s, int it0, int it1, doubl
             ++end;
         const int len = end - it;
         const UpdateParams p = params(it);
-        // launch shapes are timed on the state of the later iterations
-        tune_ready_ = tune_state(s, it);
+        // the phase whose launch shape the chunk's attraction uses
+        tune_phase_ = tune_phase(s, it);
         int grow = 0;
         while (true) {
             auto t = clk::now();

@@ -114,14 +114,14 @@ class Embedding {
                (it == 50 || it == 150 || it == 300 || it == 600 || (!reordered_ && it == it0 && it0 > 50));
     }
     int reorder_now() { return reorder(); }
-    // Whether iteration it is in the state the attraction's launch shapes are timed on: past
-    // the early exaggeration, and, when the embedding is renumbered, past the last renumbering
-    // (iteration 600).  Right after the exaggeration the embedding still expands fast and its
-    // attraction (about 1 ms at N = 1M instead of 0.7) ranks the shapes differently.
-    bool tune_state(const Schedule &s, int it) const {
-        const bool exag_done = s.stop_lying_iter < 0 || it > s.stop_lying_iter;
-        const bool renumbers = reorder_enabled_ && N_ >= kReorderMinN;
-        return exag_done && (!renumbers || it >= 600);
+    // Phase of the run for the attraction's launch shape: 0 while the embedding is compact
+    // (early exaggeration and the first 50 iterations after it), 1 once it has expanded.  The
+    // shapes rank differently in the two (N = 1M: 8 x 4 rows/edges 0.95 ms against 1.18 ms for
+    // the register-capped 16 x 2 up to iteration 260; 0.68 against 0.75 ms from 320 on), so each
+    // phase is timed on its own.  In the default schedule phase 1 starts with the renumbering
+    // at iteration 300.
+    int tune_phase(const Schedule &s, int it) const {
+        return (s.stop_lying_iter < 0 || it >= s.stop_lying_iter + 50) ? 1 : 0;
     }
     const StageTimes &last_times() const { return times_; }
     const GridGeom &last_geom() const { return geom_; }
@@ -183,8 +183,8 @@ class Embedding {
     // autotuned launch shape of the attraction pass (-1: not chosen yet); re-chosen after a
     // locality renumbering, since the gathers' locality decides between the shapes
     int attr_shape_ = -1;
-    bool attr_placeholder_ = false;  // attr_shape_ is the default, to be measured when tune_ready_
-    bool tune_ready_ = true;         // the run is past its early exaggeration
+    int attr_phase_ = -1;  // tune_phase_ that attr_shape_ was chosen for
+    int tune_phase_ = 1;   // phase of the current iteration (tune_phase)
     int tune_attr(bool measure);
     // graph chunks
     bool graphs_ = true;

@@ -155,11 +155,14 @@ def test_graph_iteration_matches_host_iteration_fp64(gpu_lib, monkeypatch, golde
 @pytest.mark.parametrize("mode", ["pipeline", "streams"])
 def test_batched_jobs_match_single_runs(gpu_lib, monkeypatch, mode):
     """fitsne_batch_run advances several embeddings together; each job ends where its own
-    fitsne_run ends (final KL within 1%), the 5,000-point job within 1% of the reference.
+    fitsne_run ends (final KL within 1% of the mean of 3 single runs), the 5,000-point job
+    within 1% of the reference.
     "pipeline": all jobs in the same launches (the default for 2-D, nterms 3, df 1);
     "streams": one graph per job on its own stream (FITSNE_BATCH=streams).
-    (Clustered data: on structureless data the final KL of two FP32 runs differs by the
-    optimiser's chaos alone, 1.2% on 1,200 isotropic Gaussian points.)"""
+    (FP32 runs differ by the optimiser's chaos alone, seeded by the order of the spread's atomic
+    additions.  Measured on the 2,500-point job: 6 single runs 1.525 - 1.535, 3 batched runs
+    1.524 - 1.537, so two single runs can be 1.2% apart; on structureless data, 1.2% on 1,200
+    isotropic Gaussian points.)"""
     if mode == "streams":
         monkeypatch.setenv("FITSNE_BATCH", "streams")
     m, g = _kl5000()
@@ -174,8 +177,9 @@ def test_batched_jobs_match_single_runs(gpu_lib, monkeypatch, mode):
     Ys, costs, st = gpu_lib.batch_run(Xs, perps, learning_rates=lrs, Y0s=Y0s, max_iter=500)
     assert st["graph_launches"] >= 9 and st["graph_instantiations"] >= 1
     for j, X in enumerate(Xs):
-        _, c = gpu_lib.run(X, Y0=Y0s[j], perplexity=perps[j], learning_rate=lrs[j], max_iter=500, knn_algo=2)
-        assert abs(costs[j][499] - c[499]) <= 1e-2 * c[499], j
+        ref = np.mean([gpu_lib.run(X, Y0=Y0s[j], perplexity=perps[j], learning_rate=lrs[j], max_iter=500,
+                                   knn_algo=2)[1][499] for _ in range(3)])
+        assert abs(costs[j][499] - ref) <= 1e-2 * ref, j
         assert np.isfinite(Ys[j]).all()
     assert abs(costs[0][499] - g["df1"][499]) <= 1e-2 * g["df1"][499]
 
