@@ -181,7 +181,8 @@ class Embedding {
     unsigned long long launches_ = 0;  // running count of this object's kernel launches
 
     // autotuned launch shape of the attraction pass (-1: not chosen yet); re-chosen after a
-    // locality renumbering, since the gathers' locality decides between the shapes
+    // locality renumbering and when the run enters a new phase, since the gathers' locality
+    // and the embedding's extent decide between the shapes
     int attr_shape_ = -1;
     int attr_phase_ = -1;  // tune_phase_ that attr_shape_ was chosen for
     int tune_phase_ = 1;   // phase of the current iteration (tune_phase)
