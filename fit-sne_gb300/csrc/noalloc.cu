@@ -11,15 +11,22 @@
 // array of fixed size, kNoAllocBytes, which every GPU that loads this library holds until
 // the process exits.
 //
-// Limits (checked, with an error message, before any device work that depends on them):
-// N <= kNoAllocMaxN points; in 2-D at most kNoAllocMaxBoxes2D boxes per dimension, in 1-D at
-// most kNoAllocMaxNodes1D interpolation nodes.
+// Layout: the per-point buffers and the reduction scratch are carved first; the grid, FFT
+// and kernel-spectrum buffers are carved after the embedding's extent has fixed the grid,
+// from its actual node count M and transform length L.  Limits (checked, with an error
+// message, before any device work that depends on them): N <= kNoAllocMaxN points; the
+// grid buffers must fit in what the per-point buffers leave of the array (in 2-D about
+// 160 (nterms * boxes)^2 bytes, in 1-D about 100 bytes per node); the transform length must
+// fit the shared-memory FFT passes (as for every other entry point).
 //
 // The array is shared by every call on a device and keeps the last call's contents: the
 // grid and the reduction counters are cleared at the start of each call.  Two calls whose
 // work overlaps on the GPU (for example on two streams) race on the array; serialise them.
-// The first call on a device looks up the array's device address (cudaGetSymbolAddress)
-// with that device current; make that first call before any stream capture.
+// The array's device address is looked up with the device current, once per CUDA context
+// (again after a device reset, which creates a new context); the first call on a device
+// does that lookup, so make it before any stream capture.
+#include <cuda.h>
+
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -36,28 +43,66 @@ namespace {
 
 constexpr size_t kNoAllocBytes = 32ull << 20;  // 32 MiB per device
 constexpr int kNoAllocMaxN = 262144;
-constexpr int kNoAllocMaxBoxes2D = 100;
-constexpr int kNoAllocMaxNodes1D = 4096;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
 std::mutex g_mu;
 void *g_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_driver_looked_up = false;
 
-// Device address of the scratch array on the current device (looked up once per device).
+// Unique id of the calling thread's current CUDA context (0 if none or unavailable).  A
+// device reset destroys the primary context; the next one gets a new id, and the array is
+// then at a new device address.
+unsigned long long current_ctx_id() {
+    if (!g_driver_looked_up) {
+        g_driver_looked_up = true;
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+            g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        }
+        cudaGetLastError();
+    }
+    if (!g_ctx_current || !g_ctx_get_id) return 0;
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (g_ctx_get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device, looked up with that device
+// current once per context.  Host code may only pass this address to kernels: the symbol
+// itself names a host-side stand-in.
 int scratch_base(void **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(FITSNE_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return set_error(FITSNE_E_ARG, "device index out of range");
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    // cudaSetDevice makes the device's primary context current on this thread, so that the
+    // context id below names the context the kernels will run in
+    e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return set_error(FITSNE_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    const unsigned long long ctx = current_ctx_id();
+    if (!g_addr[dev] || ctx == 0 || ctx != g_ctx_id[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return set_error(FITSNE_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         g_addr[dev] = p;
+        g_ctx_id[dev] = current_ctx_id();
     }
     *out = g_addr[dev];
     return 0;
@@ -105,7 +150,8 @@ extern "C" int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const un
                                            const float *d_val_P, const double *d_Y, int N, int no_dims,
                                            double *d_dC, int nterms, double intervals_per_integer,
                                            int min_num_intervals, double df, double *sum_Q, void *stream) {
-    if (!d_row_P || !d_Y || !d_dC || N < 1) return set_error(FITSNE_E_ARG, "null device buffer or N < 1");
+    if (!d_row_P || !d_col_P || !d_val_P || !d_Y || !d_dC || N < 1)
+        return set_error(FITSNE_E_ARG, "null device buffer or N < 1");
     if (N > kNoAllocMaxN)
         return set_error(FITSNE_E_ARG, "fitsne_fft_gradient_noalloc: N = " + std::to_string(N) + " exceeds the limit " +
                                            std::to_string(kNoAllocMaxN) + " of the fixed scratch array");
@@ -121,24 +167,15 @@ extern "C" int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const un
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int D = no_dims;
-    const int maxM = (D == 2) ? kNoAllocMaxBoxes2D * nterms : kNoAllocMaxNodes1D;
-    const int maxL = smooth_even_at_least(2 * maxM);
-    const size_t maxH = maxL / 2 + 1;
 
+    // per-point buffers and reduction scratch; the grid's buffers follow once its size is known
     Carve cv{static_cast<unsigned char *>(base)};
     float *Yb = cv.take<float>((size_t) N * 2 * D);
     float *rep = cv.take<float>((size_t) N * D);
     float *dCf = cv.take<float>((size_t) N * D);
-    const size_t gridn = (D == 2) ? (size_t) maxM * maxM : (size_t) maxM;
-    Cell4<float> *gin = cv.take<Cell4<float>>(gridn);
-    Cell4<float> *gout = cv.take<Cell4<float>>(gridn);
-    float2 *wa = cv.take<float2>((D == 2) ? 4 * (size_t) maxL * maxH : 6 * (size_t) maxL);
-    float2 *wb = cv.take<float2>((D == 2) ? 4 * (size_t) maxM * maxH : 1);
-    KSpec<float> *ks = cv.take<KSpec<float>>((D == 2) ? (size_t) maxL * maxH : 1);
-    float2 *tw = cv.take<float2>(maxL);
     double *red_mem = cv.take<double>(kMaxRedBlocks * 4 + 16);
     unsigned int *red_cnt = cv.take<unsigned int>(8);
-    if (cv.used > kNoAllocBytes) return set_error(FITSNE_E_ARG, "scratch layout exceeds the fixed array");
+    const size_t point_bytes = cv.used;  // <= 8.3 MiB at N = kNoAllocMaxN: fits
 
     RedScratch red;
     red.part = red_mem;
@@ -163,16 +200,34 @@ extern "C" int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const un
     gp.min_num_intervals = min_num_intervals;
     gp.df = df;
     const GridGeom g = make_grid_geom(mm[0], mm[1], D, gp);
-    if (g.M > maxM)
-        return set_error(FITSNE_E_GRID, "fitsne_fft_gradient_noalloc: the embedding needs " + std::to_string(g.nb) +
-                                            " boxes per dimension, above the fixed scratch limit");
     const int L = smooth_even_at_least(2 * g.M);
     FftPlan plan;
     if (!make_fft_plan(L, &plan)) return set_error(FITSNE_E_GRID, "bad FFT length");
+    const bool fits_fft = (D == 2) ? (L <= max_fft_len<float>())
+                                   : (2 * (size_t) L * sizeof(float2) <= 227 * 1024);
+    if (!fits_fft)
+        return set_error(FITSNE_E_GRID, "fitsne_fft_gradient_noalloc: the embedding needs " + std::to_string(g.nb) +
+                                            " boxes per dimension (transform length " + std::to_string(L) +
+                                            "), beyond the shared-memory FFT passes");
+    const size_t H = (size_t) L / 2 + 1;
+    const size_t cells = (D == 2) ? (size_t) g.M * g.M : (size_t) g.M;
+    Cell4<float> *gin = cv.take<Cell4<float>>(cells);
+    Cell4<float> *gout = cv.take<Cell4<float>>(cells);
+    float2 *wa = cv.take<float2>((D == 2) ? 4 * (size_t) L * H : 6 * (size_t) L);
+    float2 *wb = cv.take<float2>((D == 2) ? 4 * (size_t) g.M * H : 1);
+    KSpec<float> *ks = cv.take<KSpec<float>>((D == 2) ? (size_t) L * H : 1);
+    float2 *tw = cv.take<float2>(L);
+    if (cv.used > kNoAllocBytes)
+        return set_error(FITSNE_E_GRID,
+                         "fitsne_fft_gradient_noalloc: N = " + std::to_string(N) + " and a grid of " +
+                             std::to_string(g.nb) + " boxes per dimension x " + std::to_string(nterms) +
+                             " nodes need " + std::to_string(point_bytes) + " + " +
+                             std::to_string(cv.used - point_bytes) + " bytes of scratch; the fixed array holds " +
+                             std::to_string(kNoAllocBytes));
+
     const int mode = (df == 1.0) ? KERNEL_DF1 : KERNEL_VARDF;
     k_twiddles<<<(L + 255) / 256, 256, 0, st>>>(tw, L);
     NCK(cudaGetLastError());
-    const size_t cells = (D == 2) ? (size_t) g.M * g.M : (size_t) g.M;
     NCK(cudaMemsetAsync(gin, 0, sizeof(Cell4<float>) * cells, st));
     NCK(launch_spread<float>(Yb, N, D, g, gin, st));
     if (D == 2)
@@ -188,9 +243,9 @@ extern "C" int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const un
                                   st));
     k_f2d<<<256, 256, 0, st>>>(dCf, d_dC, (size_t) N * D);
     NCK(cudaGetLastError());
-    if (sum_Q) {
-        NCK(cudaMemcpyAsync(sum_Q, red.z, sizeof(double), cudaMemcpyDeviceToHost, st));
-        NCK(cudaStreamSynchronize(st));
-    }
+    double z = 0.0;
+    NCK(cudaMemcpyAsync(&z, red.z, sizeof(double), cudaMemcpyDeviceToHost, st));
+    NCK(cudaStreamSynchronize(st));
+    if (sum_Q) *sum_Q = z;
     return 0;
 }

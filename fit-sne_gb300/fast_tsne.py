@@ -10,8 +10,9 @@ package's GPU build.  Usage is unchanged::
 
 Differences: knn_algo='annoy' (the reference default) is served by the exact GPU kNN;
 nbody_algo='Barnes-Hut' and theta=0 (exact t-SNE) are outside this build and make the
-binary exit with an error.  PCA initialisation uses scikit-learn when it is installed
-(exactly as the reference) and an equivalent NumPy SVD otherwise.
+binary exit with an error.  PCA initialisation runs on the GPU (``fitsne.pca``: the
+covariance's leading eigenvectors with scikit-learn's sign rule); ``FITSNE_PCA=sklearn``
+uses scikit-learn's PCA instead, as the reference does.
 """
 from __future__ import annotations
 

@@ -162,16 +162,21 @@ void fitsne_session_destroy(fitsne_session *s);
  * Same computation and result as fitsne_fft_gradient in the FP32 form, on the caller's
  * DEVICE buffers: d_row_P[N+1], d_col_P[nnz], d_val_P[nnz] (float), d_Y[N*no_dims] (double)
  * in; d_dC[N*no_dims] (double) out; *sum_Q (host, may be NULL) receives Z.  stream is a
- * cudaStream_t (NULL = the legacy default stream); the call returns after a host
- * synchronisation on it.  All temporaries come from one fixed device array of 32 MiB that
- * every GPU loading this library holds until the process exits.  Limits: N <= 262144;
- * at most 100 boxes per dimension in 2-D (the embedding's extent / intervals_per_integer,
- * or min_num_intervals, must stay at or below 100) and at most 4096 interpolation nodes in
- * 1-D; larger inputs are rejected with FITSNE_E_ARG or FITSNE_E_GRID and a message.  The
- * array is shared by all calls on a device and keeps the last call's contents (each call
- * clears what must start at zero): calls whose work overlaps on the GPU race on it.  The
- * first call on a device looks up the array's address with that device current; make it
- * before any stream capture. */
+ * cudaStream_t (NULL = the legacy default stream).  The call synchronises the host with
+ * that stream twice: once to read the embedding's extent, which sizes the grid, and once
+ * before it returns, when its work is complete.  All temporaries come from one fixed device
+ * array of 32 MiB that every GPU loading this library holds until the process exits.
+ * Limits: N <= 262144; the per-point buffers (32 N bytes in 2-D) and the grid's buffers
+ * (about 160 (n_interpolation_points x boxes per dimension)^2 bytes in 2-D, about 100 bytes
+ * per node in 1-D) must fit in the array together.  At N = 262144 that allows, per
+ * dimension, 128 boxes at n_interpolation_points 3, 76 at 5 and 48 at 8 (a little more for
+ * fewer points); the box count is the embedding's extent / intervals_per_integer, at least
+ * min_num_intervals.  Larger inputs are rejected with FITSNE_E_ARG (N) or FITSNE_E_GRID
+ * (grid) and a message naming the sizes.  The array is shared by all calls on a device and
+ * keeps the last call's contents (each call clears what must start at zero): calls whose
+ * work overlaps on the GPU race on it.  The array's device address is looked up with the
+ * device current, once per CUDA context; the first call on a device does that lookup, so
+ * make it before any stream capture. */
 int fitsne_fft_gradient_noalloc(const unsigned int *d_row_P, const unsigned int *d_col_P, const float *d_val_P,
                                 const double *d_Y, int N, int no_dims, double *d_dC, int nterms,
                                 double intervals_per_integer, int min_num_intervals, double df, double *sum_Q,
@@ -217,7 +222,10 @@ int fitsne_get_calibration(void);
 /* Statistics of this process's last calibration, out[12]: rows, harvested rows (plain
  * bisection), predicted rows that needed bisection steps, training steps, mean entropy
  * evaluations per harvested row, mean per predicted row, first and last training loss
- * (standardised MSE), ms for harvest, training, inference, warm-started search.  Returns 0. */
+ * (standardised MSE), ms for harvest (with the plain bisection: of all rows), training,
+ * inference, warm-started search.  Entropy evaluations count FP32 and FP64 steps alike
+ * (both searches evaluate a step in FP32 first and in FP64 where FP32 cannot decide it).
+ * Returns 0. */
 int fitsne_calibration_stats(double *out12);
 /* Number of FP32 parameters of the network for K distances per row: W1[64][K], b1[64],
  * W2[64][64], b2[64], w3[64], b3. */

@@ -52,15 +52,46 @@ def test_noalloc_gradient_matches_allocating_entry_point(gpu_lib, golden, yk, df
         assert abs(z - zref) <= 1e-5 * abs(zref)
 
 
+@pytest.mark.parametrize("nterms", [5, 8])
+def test_noalloc_gradient_at_more_interpolation_points(gpu_lib, golden, nterms):
+    """The grid buffers are carved from the actual grid, so a small embedding works at any
+    n_interpolation_points; nterms = 5 is also checked against the reference's gradient."""
+    lib = gpu_lib.lib()
+    row, col = golden["sym_row"], golden["sym_col"]
+    val = golden["sym_val"] / golden["sym_val"].sum()
+    Y = golden["Y2"]
+    # nterms = 5 on the reference fixture's grid parameters (intervals_per_integer 2,
+    # min_num_intervals 30); nterms = 8 on the defaults
+    ipi, min_int = (2.0, 30) if nterms == 5 else (1.0, 50)
+    gpu_lib.set_precision(32)
+    ref, zref = gpu_lib.fft_gradient(row, col, val, Y, nterms, ipi, min_int, 1.0)
+    for _ in range(2):
+        rc, dC, z = _noalloc(lib, row, col, val, Y, 1.0, nterms=nterms, ipi=ipi, min_int=min_int)
+        assert rc == 0, lib.fitsne_last_error()
+        assert rel_l2(dC, ref) < 1e-4
+        assert abs(z - zref) <= 1e-5 * abs(zref)
+        if nterms == 5:
+            assert rel_l2(dC, golden["g2_nt5_dC"]) < 1e-4
+            assert abs(z - float(golden["g2_nt5_Z"])) <= 1e-5 * float(golden["g2_nt5_Z"])
+
+
 def test_noalloc_rejects_inputs_beyond_its_limits(gpu_lib, golden):
     lib = gpu_lib.lib()
     row, col = golden["sym_row"], golden["sym_col"]
     val = golden["sym_val"] / golden["sym_val"].sum()
-    # an embedding too wide for 100 boxes per dimension
-    rc, _, _ = _noalloc(lib, row, col, val, golden["Y2"] * 20.0, 1.0)
-    assert rc == -13 and b"boxes" in lib.fitsne_last_error()
-    # too many points (checked before any device work)
-    rc = lib.fitsne_fft_gradient_noalloc(ctypes.c_void_p(1), ctypes.c_void_p(1), ctypes.c_void_p(1),
-                                         ctypes.c_void_p(1), 300000, 2, ctypes.c_void_p(1), 3, 1.0, 50, 1.0, None,
-                                         None)
+    # a grid too large for the fixed array: 160 boxes per dimension x 8 nodes
+    rc, _, _ = _noalloc(lib, row, col, val, golden["Y2"], 1.0, nterms=8, min_int=160)
+    assert rc == -13 and b"scratch" in lib.fitsne_last_error()
+    # too many points: real (small) device buffers, so that no check order can hand a
+    # kernel an invalid address; the N check rejects the call before any device work
+    d_row = torch.zeros(16, dtype=torch.int32, device="cuda")
+    d_col = torch.zeros(16, dtype=torch.int32, device="cuda")
+    d_val = torch.zeros(16, dtype=torch.float32, device="cuda")
+    d_Y = torch.zeros(16, dtype=torch.float64, device="cuda")
+    d_dC = torch.zeros(16, dtype=torch.float64, device="cuda")
+    rc = lib.fitsne_fft_gradient_noalloc(d_row.data_ptr(), d_col.data_ptr(), d_val.data_ptr(), d_Y.data_ptr(),
+                                         300000, 2, d_dC.data_ptr(), 3, 1.0, 50, 1.0, None, None)
     assert rc == -3 and b"exceeds" in lib.fitsne_last_error()
+    # null buffers are rejected as argument errors
+    rc = lib.fitsne_fft_gradient_noalloc(None, None, None, None, 100, 2, None, 3, 1.0, 50, 1.0, None, None)
+    assert rc == -3
