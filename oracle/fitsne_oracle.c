@@ -939,6 +939,50 @@ static double randn_polar(void) {
     return x;
 }
 
+/* The optimisation loop of TSNE::run (src/tsne.cpp:389-577): auto early exaggeration,
+ * val scaled in place by the exaggeration, the update, zero-mean, the schedule switches
+ * after each iteration's update, KL every 50 iterations with the stale Z (quirk Q6). */
+static void optimise(unsigned *row, unsigned *col, double *val, int N, double *Y, int no_dims, int max_iter,
+                     int stop_lying_iter, int mom_switch_iter, double momentum, double final_momentum,
+                     double learning_rate, double early_exag_coeff, double *costs, int no_momentum_during_exag,
+                     int start_late_exag_iter, double late_exag_coeff, int nterms, double ipi, int min_int,
+                     unsigned int nthreads, double df, double max_step_norm, double *dY, double *uY, double *gains) {
+    if (early_exag_coeff == 0) {
+        double mxs = 0;
+        for (int n = 0; n < N; n++) {
+            double s = 0;
+            for (unsigned i = row[n]; i < row[n + 1]; i++) s += val[i];
+            if (s > mxs) mxs = s;
+        }
+        early_exag_coeff = (1.0 / (learning_rate * mxs));
+    }
+    for (unsigned i = 0; i < row[N]; i++) val[i] *= early_exag_coeff;
+    for (int iter = 0; iter < max_iter; iter++) {
+        /* Z of this iteration's gradient is the current_sum_Q the cost uses */
+        const double zq = orc_fft_gradient(row, col, val, Y, N, no_dims, dY, nterms, ipi, min_int, nthreads, df);
+        if (no_momentum_during_exag) {
+            if (iter > stop_lying_iter) update(Y, uY, gains, dY, N, no_dims, 1, 0, momentum, learning_rate, -1.0);
+            else update(Y, uY, gains, dY, N, no_dims, 0, 1, momentum, learning_rate, -1.0);
+        } else {
+            update(Y, uY, gains, dY, N, no_dims, 1, 0, momentum, learning_rate, max_step_norm);
+        }
+        zero_mean(Y, N, no_dims);
+        if (iter == stop_lying_iter)
+            for (unsigned i = 0; i < row[N]; i++) val[i] /= early_exag_coeff;
+        if (iter == start_late_exag_iter)
+            for (unsigned i = 0; i < row[N]; i++) val[i] *= late_exag_coeff;
+        if (iter == mom_switch_iter) momentum = final_momentum;
+        if ((iter + 1) % 50 == 0 || iter == max_iter - 1) {
+            double C = orc_evaluate_error_fft(row, col, val, Y, N, no_dims, df, zq);
+            if (iter < stop_lying_iter && stop_lying_iter != -1)
+                C = C / early_exag_coeff - log(early_exag_coeff);
+            if (iter >= start_late_exag_iter && start_late_exag_iter != -1)
+                C = C / late_exag_coeff - log(late_exag_coeff);
+            costs[iter] = C;
+        }
+    }
+}
+
 /* ---------------------------------------------------------------------------------
  * TSNE::run restricted to the FFT path (src/tsne.cpp:118-592): theta != 0, nbody 2,
  * exact kNN (knn_algo 1 is served by the same VP-tree), no P-file I/O. */
@@ -992,46 +1036,45 @@ int orc_run(double *X, int N, int D, double *Y, int no_dims, double perplexity, 
         srand(rand_seed >= 0 ? (unsigned) rand_seed : (unsigned) time(NULL));
         for (size_t i = 0; i < nd; i++) Y[i] = randn_polar() * .0001;
     }
-    if (early_exag_coeff == 0) {
-        double mxs = 0;
-        for (int n = 0; n < N; n++) {
-            double s = 0;
-            for (unsigned i = row[n]; i < row[n + 1]; i++) s += val[i];
-            if (s > mxs) mxs = s;
-        }
-        early_exag_coeff = (1.0 / (learning_rate * mxs));
-    }
-    for (unsigned i = 0; i < row[N]; i++) val[i] *= early_exag_coeff;
-    for (int iter = 0; iter < max_iter; iter++) {
-        /* Z of this iteration's gradient is the current_sum_Q the cost uses */
-        const double zq = orc_fft_gradient(row, col, val, Y, N, no_dims, dY, nterms, ipi, min_int, nthreads, df);
-        if (no_momentum_during_exag) {
-            if (iter > stop_lying_iter) update(Y, uY, gains, dY, N, no_dims, 1, 0, momentum, learning_rate, -1.0);
-            else update(Y, uY, gains, dY, N, no_dims, 0, 1, momentum, learning_rate, -1.0);
-        } else {
-            update(Y, uY, gains, dY, N, no_dims, 1, 0, momentum, learning_rate, max_step_norm);
-        }
-        zero_mean(Y, N, no_dims);
-        if (iter == stop_lying_iter)
-            for (unsigned i = 0; i < row[N]; i++) val[i] /= early_exag_coeff;
-        if (iter == start_late_exag_iter)
-            for (unsigned i = 0; i < row[N]; i++) val[i] *= late_exag_coeff;
-        if (iter == mom_switch_iter) momentum = final_momentum;
-        if ((iter + 1) % 50 == 0 || iter == max_iter - 1) {
-            double C = orc_evaluate_error_fft(row, col, val, Y, N, no_dims, df, zq);
-            if (iter < stop_lying_iter && stop_lying_iter != -1)
-                C = C / early_exag_coeff - log(early_exag_coeff);
-            if (iter >= start_late_exag_iter && start_late_exag_iter != -1)
-                C = C / late_exag_coeff - log(late_exag_coeff);
-            costs[iter] = C;
-        }
-    }
+    optimise(row, col, val, N, Y, no_dims, max_iter, stop_lying_iter, mom_switch_iter, momentum, final_momentum,
+             learning_rate, early_exag_coeff, costs, no_momentum_during_exag, start_late_exag_iter, late_exag_coeff,
+             nterms, ipi, min_int, nthreads, df, max_step_norm, dY, uY, gains);
     free(dY);
     free(uY);
     free(gains);
     free(row);
     free(col);
     free(val);
+    return 0;
+}
+
+/* TSNE::run with load_affinities = 1 (src/tsne.cpp:236-281): the loop on a given P (the
+ * symmetrised, normalised matrix the reference saves with load_affinities = 2) from the
+ * given Y.  val is copied: the loop scales its P in place. */
+int orc_run_from_P(const unsigned *row, const unsigned *col, const double *val, int N, double *Y, int no_dims,
+                   int max_iter, int stop_lying_iter, int mom_switch_iter, double momentum, double final_momentum,
+                   double learning_rate, double early_exag_coeff, double *costs, int no_momentum_during_exag,
+                   int start_late_exag_iter, double late_exag_coeff, int nterms, double ipi, int min_int,
+                   unsigned int nthreads, double df, double max_step_norm) {
+    const size_t nd = (size_t) N * no_dims, nnz = row[N];
+    unsigned *r = (unsigned *) malloc(sizeof(unsigned) * (N + 1));
+    unsigned *c = (unsigned *) malloc(sizeof(unsigned) * (nnz ? nnz : 1));
+    double *v = (double *) malloc(sizeof(double) * (nnz ? nnz : 1));
+    memcpy(r, row, sizeof(unsigned) * (N + 1));
+    memcpy(c, col, sizeof(unsigned) * nnz);
+    memcpy(v, val, sizeof(double) * nnz);
+    double *dY = (double *) malloc(sizeof(double) * nd), *uY = (double *) calloc(nd, sizeof(double));
+    double *gains = (double *) malloc(sizeof(double) * nd);
+    for (size_t i = 0; i < nd; i++) gains[i] = 1.0;
+    optimise(r, c, v, N, Y, no_dims, max_iter, stop_lying_iter, mom_switch_iter, momentum, final_momentum,
+             learning_rate, early_exag_coeff, costs, no_momentum_during_exag, start_late_exag_iter, late_exag_coeff,
+             nterms, ipi, min_int, nthreads, df, max_step_norm, dY, uY, gains);
+    free(dY);
+    free(uY);
+    free(gains);
+    free(r);
+    free(c);
+    free(v);
     return 0;
 }
 

@@ -38,8 +38,18 @@ def build_restated(force: bool = False) -> str:
     return RESTATED_LIB
 
 
-def build_reference(ref_root: str = "/root/reference") -> str | None:
+def reference_dir() -> str:
+    """The FIt-SNE checkout: $FITSNE_REFERENCE_DIR when set, else a directory named
+    ``reference`` beside this repository."""
+    env = os.environ.get("FITSNE_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+def build_reference(ref_root: str | None = None) -> str | None:
     """Compiles the reference checker when the reference tree exists; else None."""
+    ref_root = ref_root or reference_dir()
     if not os.path.isdir(os.path.join(ref_root, "src")):
         return REF_LIB if os.path.exists(REF_LIB) else None
     subprocess.run(["make", "-C", HERE, "ref", "REF=" + ref_root], check=True, capture_output=True)
@@ -158,7 +168,7 @@ class _Common:
             momentum=0.5, final_momentum=0.8, learning_rate=200.0, K=-1, sigma=-1.0, early_exag_coeff=12.0,
             no_momentum_during_exag=0, start_late_exag_iter=-1, late_exag_coeff=-1.0, nterms=3, ipi=1.0,
             min_num_intervals=50, nthreads=1, perplexity_list=None, df=1.0, max_step_norm=5.0, knn_algo=2,
-            rand_seed=-1):
+            rand_seed=-1, load_affinities=0):
         X = np.ascontiguousarray(X, np.float64).copy()
         N, D = X.shape
         skip = Y0 is not None
@@ -172,7 +182,7 @@ class _Common:
                              max_iter, stop_lying_iter, mom_switch_iter, momentum, final_momentum, learning_rate, K,
                              sigma, 2, knn_algo, early_exag_coeff, _p(costs, _f64p), int(no_momentum_during_exag),
                              start_late_exag_iter, late_exag_coeff, 50, -1, nterms, ipi, min_num_intervals,
-                             nthreads, 0, npl, _p(pl, _f64p), df, max_step_norm)
+                             nthreads, int(load_affinities), npl, _p(pl, _f64p), df, max_step_norm)
         if rc != 0:
             raise RuntimeError("run returned %d" % rc)
         return Y, costs
@@ -207,6 +217,12 @@ class Restated(_Common):
         L = self.lib
         L.orc_knn.restype = None
         L.orc_knn.argtypes = [_f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _u32p, _f64p, ctypes.c_int]
+        L.orc_run_from_P.restype = ctypes.c_int
+        L.orc_run_from_P.argtypes = [_u32p, _u32p, _f64p, ctypes.c_int, _f64p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, _f64p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint, ctypes.c_double,
+                                     ctypes.c_double]
         L.orc_gradient_step.restype = ctypes.c_int
         L.orc_gradient_step.argtypes = [_u32p, _u32p, _f64p, _f64p, _f64p, _f64p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_uint,
@@ -221,6 +237,25 @@ class Restated(_Common):
         dist = np.zeros((N, K))
         self.lib.orc_knn(_p(X, _f64p), N, D, K, _p(idx, _u32p), _p(dist, _f64p), nthreads)
         return idx, dist
+
+    def run_from_P(self, row, col, val, Y0, max_iter=1000, stop_lying_iter=250, mom_switch_iter=250, momentum=0.5,
+                   final_momentum=0.8, learning_rate=200.0, early_exag_coeff=12.0, no_momentum_during_exag=0,
+                   start_late_exag_iter=-1, late_exag_coeff=-1.0, nterms=3, ipi=1.0, min_num_intervals=50,
+                   nthreads=1, df=1.0, max_step_norm=5.0):
+        """TSNE::run's loop on a given (symmetrised, normalised) P from Y0, as with
+        load_affinities = 1: returns (Y, costs)."""
+        row, col, val = _csr(row, col, val)
+        Y = np.ascontiguousarray(Y0, np.float64).copy()
+        if Y.ndim == 1:
+            Y = Y[:, None]
+        N, d = Y.shape
+        costs = np.zeros(max(1, max_iter))
+        self.lib.orc_run_from_P(_p(row, _u32p), _p(col, _u32p), _p(val, _f64p), N, _p(Y, _f64p), d, max_iter,
+                                stop_lying_iter, mom_switch_iter, momentum, final_momentum, learning_rate,
+                                early_exag_coeff, _p(costs, _f64p), int(no_momentum_during_exag),
+                                start_late_exag_iter, late_exag_coeff, nterms, ipi, min_num_intervals, nthreads, df,
+                                max_step_norm)
+        return Y, costs
 
     def gradient_step(self, row, col, val, Y, uY, gains, nterms=3, ipi=1.0, min_num_intervals=50, nthreads=1,
                       df=1.0, exag=1.0, momentum=0.5, learning_rate=200.0, use_gains=1, max_step_norm=5.0):

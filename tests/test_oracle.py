@@ -93,6 +93,23 @@ def test_restated_run_matches_reference_fixture(orc, golden):
     assert np.allclose(costs[idx], golden["e2e_costs"][idx], rtol=1e-9)
 
 
+def test_restated_loop_on_a_given_P_matches_reference_fixture(orc, golden):
+    """The loop alone (TSNE::run with load_affinities = 1) on the P the reference builds
+    (X centred and scaled by its largest magnitude, VP-tree kNN, calibration,
+    symmetrisation, normalisation) reproduces the reference's run."""
+    X = golden["e2e_X"]
+    X = X - np.cumsum(X, axis=0)[-1] / len(X)  # zeroMean's sequential column sums
+    X = X / np.abs(X).max()
+    r, c, v = orc.gaussian_perplexity(X, 15.0, 45, nthreads=2)
+    r, c, v = orc.symmetrize(r, c, v, len(X))
+    v = v / np.cumsum(v)[-1]  # the reference's sequential sum of P
+    Y, costs = orc.run_from_P(r, c, v, golden["e2e_Y0"], max_iter=300, stop_lying_iter=100, mom_switch_iter=100,
+                              learning_rate=200.0, nthreads=2)
+    assert np.abs(Y - golden["e2e_Y"]).max() <= 1e-9
+    idx = [49, 99, 149, 199, 249, 299]
+    assert np.allclose(costs[idx], golden["e2e_costs"][idx], rtol=1e-9)
+
+
 def test_restated_knn_is_exact(orc, golden):
     X = golden["sim_X"][:600]
     idx, dist = orc.knn(X, 11, 2)
