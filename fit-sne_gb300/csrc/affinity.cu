@@ -67,12 +67,55 @@ __global__ void k_scale(double *__restrict__ X, size_t n, const unsigned long lo
 
 // ---------------------------------------------------------------------------------
 // perplexity calibration, one thread per row, sums in the reference's order
-// Re-evaluates P for the beta at which the reference stopped.  The reference computes P
-// inside the loop before testing, so P corresponds to the beta of the last evaluation;
-// this helper reproduces that beta and writes the normalised row.
+// (distances2similarities, src/tsne.cpp:1394-1469).
+//
+// The bisection is bound by the FP64 pipe (GB300 runs FP64 at a small fraction of its FP32
+// rate): every step evaluates K exponentials.  But a step's outcome is only which way the
+// bracket moves, and the sequence of betas is fixed by those outcomes.  So each step is
+// first evaluated in FP32 on the row's distances shifted by their minimum, with a bound on
+// that value's error; when the FP32 value decides the outcome for certain (|H - log U| is
+// farther from tol than the bound), the step takes it; otherwise the step is evaluated in
+// FP64 exactly as the reference does.  The betas visited, the number of steps and P (the
+// FP64 row of the last evaluation, which is always an FP64 one when the bisection
+// converges) are therefore the reference's, bit for bit.
+
+// One bisection step in FP32: +1 when H(beta) - logU > tol for certain, -1 when it is below
+// -tol for certain, 0 when the FP32 value cannot decide.  s[m * sstride] holds the row's
+// distances minus their minimum d0, rounded to FP32.
+//   H = beta sum(d e) / sum(e) + log sum(e) = beta sum(t e') / sum(e') + log sum(e'),
+// with t = d - d0 and e' = exp(-beta t), so both terms are non-negative (sum(e') >= 1) and
+// no cancellation occurs.  Error bound: each e' carries 1.8e-7 |x| + 2.4e-7 relative error
+// (x = -beta t with beta and t rounded to FP32; expf within 2 ulp), the sequential sums
+// K 2^-24 relative; with sum(e') >= 1, |x| e^-|x| <= 1/e and |x|^2 e^-|x| <= 4/e^2 the
+// absolute error of H stays below (3.6e-7 K + 3e-7)(1 + H).  The bound used is
+// (5e-7 K + 2e-6)(1 + H) + 1e-9.  The shifted form is the reference's value only while
+// exp(-beta d0) is far from FP64 underflow, where the
+// reference's DBL_MIN seed of sum_P matters: beyond beta d0 = 600 the step goes to FP64.
+__device__ __forceinline__ int screen_step(const float *__restrict__ s, int sstride, int K, double beta, double d0,
+                                           double logU, double tol) {
+    if (!(beta > 1e-30 && beta < 1e30) || beta * d0 > 600.0) return 0;
+    const float bf = (float) beta;
+    float B = 0.f, A = 0.f;
+    for (int m = 0; m < K; ++m) {
+        const float t = s[(size_t) m * sstride];
+        const float e = expf(-bf * t);
+        B += e;
+        A = fmaf(t, e, A);
+    }
+    const float h = bf * (A / B) + logf(B);
+    const double E = (5e-7 * K + 2e-6) * (1.0 + fabs((double) h)) + 1e-9;
+    const double Hd = (double) h - logU;
+    if (Hd > tol + E) return 1;
+    if (Hd < -(tol + E)) return -1;
+    return 0;
+}
+
+// Calibrates one row.  s (may be null: FP64 steps only) is the row's FP32 shifted copy for
+// screen_step; d0 the row's smallest distance.  Writes the normalised row p and returns the
+// beta the reference's loop returns.
 __device__ double calibrate_row(const double *__restrict__ d, double *__restrict__ p, int K, double perplexity,
-                                double sigma, int *evals = nullptr) {
-    double beta_eval;
+                                double sigma, int *evals = nullptr, const float *__restrict__ s = nullptr,
+                                int sstride = 0, double d0 = 0.0) {
     if (perplexity > 0) {
         double min_beta = -DBL_MAX, max_beta = DBL_MAX;
         const double tol = 1e-5;
@@ -80,20 +123,31 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
         bool found = false;
         int iter = 0;
         double beta = 1.0;
-        beta_eval = beta;
+        double beta_eval = beta;
+        bool last_fp64 = false;  // p holds exp(-beta_eval d) and last_sum their sum
+        double last_sum = DBL_MIN;
         while (!found && iter < 200) {
             beta_eval = beta;
-            double sum_P = DBL_MIN, H = 0.0;
-            for (int m = 0; m < K; ++m) {
-                const double e = exp(-beta * d[m]);
-                sum_P += e;
-                H += beta * (d[m] * e);
+            int dir = s ? screen_step(s, sstride, K, beta, d0, logU, tol) : 0;
+            last_fp64 = (dir == 0);
+            if (dir == 0) {
+                double sum_P = DBL_MIN, H = 0.0;
+                for (int m = 0; m < K; ++m) {
+                    const double e = exp(-beta * d[m]);
+                    p[m] = e;
+                    sum_P += e;
+                    H += beta * (d[m] * e);
+                }
+                H = (H / sum_P) + log(sum_P);
+                last_sum = sum_P;
+                const double Hdiff = H - logU;
+                if (Hdiff < tol && -Hdiff < tol)
+                    found = true;
+                else
+                    dir = Hdiff > 0 ? 1 : -1;
             }
-            H = (H / sum_P) + log(sum_P);
-            const double Hdiff = H - logU;
-            if (Hdiff < tol && -Hdiff < tol) {
-                found = true;
-            } else if (Hdiff > 0) {
+            if (found) {
+            } else if (dir > 0) {
                 min_beta = beta;
                 if (max_beta == DBL_MAX || max_beta == -DBL_MAX)
                     beta *= 2.0;
@@ -111,15 +165,17 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
         if (evals) *evals = iter;
         // P of the reference is the row evaluated at beta_eval; the returned beta is the
         // updated one when the loop ran out of iterations (as in the reference)
-        double sum_P = DBL_MIN;
-        for (int m = 0; m < K; ++m) {
-            p[m] = exp(-beta_eval * d[m]);
-            sum_P += p[m];
+        if (!last_fp64) {
+            last_sum = DBL_MIN;
+            for (int m = 0; m < K; ++m) {
+                p[m] = exp(-beta_eval * d[m]);
+                last_sum += p[m];
+            }
         }
-        for (int m = 0; m < K; ++m) p[m] /= sum_P;
+        for (int m = 0; m < K; ++m) p[m] /= last_sum;
         return beta;
     }
-    beta_eval = 1 / (2 * sigma * sigma);
+    const double beta_eval = 1 / (2 * sigma * sigma);
     double sum_P = DBL_MIN;
     for (int m = 0; m < K; ++m) {
         p[m] = exp(-beta_eval * d[m]);
@@ -129,23 +185,36 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
     return beta_eval;
 }
 
+// Rows of the block in shared memory as FP32 shifted distances, one column per thread
+// ([m][thread]: the lanes of a warp read consecutive words), when the launch provides the
+// space (stage = 1); the FP64 distances stay in global memory (read only by FP64 steps).
 __global__ void k_calibrate(const double *__restrict__ dist, int stride, int offset, double *__restrict__ P,
                             double *__restrict__ tmp, int nrows, int K, double perplexity, double sigma,
                             const double *__restrict__ list, int list_len, double *__restrict__ beta_out,
-                            int *__restrict__ evals_out) {
+                            int *__restrict__ evals_out, int stage) {
+    extern __shared__ float s_shift[];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
     const double *d = dist + (size_t) r * stride + offset;
     double *p = P + (size_t) r * K;
+    const float *s = nullptr;
+    double d0 = 0.0;
+    if (stage && perplexity >= 0) {
+        d0 = d[0];
+        for (int m = 1; m < K; ++m) d0 = fmin(d0, d[m]);
+        float *w = s_shift + threadIdx.x;
+        for (int m = 0; m < K; ++m) w[(size_t) m * blockDim.x] = (float) (d[m] - d0);
+        s = w;
+    }
     double beta;
     int evals = 0;
     if (perplexity != 0) {
-        beta = calibrate_row(d, p, K, perplexity, sigma, &evals);
+        beta = calibrate_row(d, p, K, perplexity, sigma, &evals, s, blockDim.x, d0);
     } else {
         double *t = tmp + (size_t) r * K;
-        beta = calibrate_row(d, p, K, list[0], sigma, &evals);
+        beta = calibrate_row(d, p, K, list[0], sigma, &evals, s, blockDim.x, d0);
         for (int m = 1; m < list_len; ++m) {
-            beta = calibrate_row(d, t, K, list[m], sigma);
+            beta = calibrate_row(d, t, K, list[m], sigma, nullptr, s, blockDim.x, d0);
             for (int i = 0; i < K; ++i) p[i] += t[i];
         }
         for (int i = 0; i < K; ++i) p[i] /= list_len;
@@ -517,8 +586,16 @@ int calibrate_rows(const double *dist, int stride, int offset, double *P, int nr
         ACK(cudaMemcpyAsync(list, list_host, sizeof(double) * list_len, cudaMemcpyHostToDevice, st));
         ACK(cudaMalloc(&tmp, sizeof(double) * (size_t) nrows * K));
     }
-    k_calibrate<<<(nrows + 127) / 128, 128, 0, st>>>(dist, stride, offset, P, tmp, nrows, K, perplexity, sigma, list,
-                                                      list_len, beta, evals);
+    // FP32 shifted rows in shared memory: 128 rows per block up to K = 320, fewer rows for
+    // longer ones, none (FP64 steps only) beyond K = 1280
+    int bd = 128;
+    while (bd > 32 && (size_t) bd * K * sizeof(float) > 160 * 1024) bd /= 2;
+    const size_t smem = (size_t) bd * K * sizeof(float);
+    const int stage = smem <= 160 * 1024 ? 1 : 0;
+    if (stage) ACK(cudaFuncSetAttribute(k_calibrate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    k_calibrate<<<(nrows + bd - 1) / bd, bd, stage ? smem : 0, st>>>(dist, stride, offset, P, tmp, nrows, K,
+                                                                      perplexity, sigma, list, list_len, beta, evals,
+                                                                      stage);
     ACK(cudaGetLastError());
     if (iters) {
         iters->resize(nrows);
@@ -583,6 +660,7 @@ int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double per
         if (!rc) {
             MlpStats ms;
             ms.rows = ms.rows_harvest = N;
+            ms.ms_harvest = (now_s() - t1) * 1e3;  // every row takes the bisection
             double s = 0;
             for (int v : evals) s += v;
             ms.iters_plain = N ? s / N : 0;

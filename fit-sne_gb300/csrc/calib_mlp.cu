@@ -235,9 +235,18 @@ size_t infer_smem(int K) {
 // DBL_MIN), decreasing in beta, dH/dbeta = -beta Var(d).  The bracket [lo, hi] shrinks with
 // every evaluation; a Newton step that leaves it, or a missing prediction, is replaced by
 // doubling / bisection as in the reference.
+//
+// The first steps run in FP32 on the row's distances shifted by their minimum (staged in
+// shared memory, one column per thread), where H = beta <t> + log sum exp(-beta t) has no
+// cancellation and a bound on its error (the one of the bisection's FP32 screen): a step
+// moves the bracket only when the sign of H - log U is certain, and the FP32 phase ends when
+// |H - log U| is within that bound.  The FP64 steps that follow take the row to the
+// acceptance test |H - log U| < 1e-6; each writes exp(-beta d) to the output row, so the
+// accepted evaluation's values only need the normalisation.
 __global__ void k_calibrate_warm(const double *__restrict__ dist, int stride, int offset, double *__restrict__ P,
                                  int nrows, int K, double perplexity, const double *__restrict__ beta_hat,
-                                 int *__restrict__ iters, int *__restrict__ fallback) {
+                                 int *__restrict__ iters, int *__restrict__ fallback, int stage) {
+    extern __shared__ float s_shift[];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
     const double *d = dist + (size_t) r * stride + offset;
@@ -250,19 +259,58 @@ __global__ void k_calibrate_warm(const double *__restrict__ dist, int stride, in
         beta = 1.0;
         fb = 1;
     }
-    double lo = 0.0, hi = HUGE_VAL, beta_eval = beta;
+    double lo = 0.0, hi = HUGE_VAL;
     int it = 0;
-    while (it < 200) {
-        beta_eval = beta;
+    if (stage) {
+        double d0 = d[0];
+        for (int m = 1; m < K; ++m) d0 = fmin(d0, d[m]);
+        float *w = s_shift + threadIdx.x;
+        const size_t sst = blockDim.x;
+        for (int m = 0; m < K; ++m) w[m * sst] = (float) (d[m] - d0);
+        while (it < 30 && beta > 1e-30 && beta < 1e30 && beta * d0 <= 600.0) {
+            const float bf = (float) beta;
+            float B = 0.f, A1 = 0.f, A2 = 0.f;
+            for (int m = 0; m < K; ++m) {
+                const float t = w[m * sst];
+                const float e = expf(-bf * t);
+                B += e;
+                A1 = fmaf(t, e, A1);
+                A2 = fmaf(t * t, e, A2);
+            }
+            ++it;
+            const float mt = A1 / B;
+            const float h = bf * mt + logf(B);
+            const double f = (double) h - logU;
+            const double E = (5e-7 * K + 2e-6) * (1.0 + fabs((double) h)) + 1e-9;
+            if (fabs(f) <= E + tol) break;  // FP32 cannot resolve further: FP64 from here
+            if (f > 0.0)
+                lo = beta;
+            else
+                hi = beta;
+            const double dH = -beta * ((double) (A2 / B) - (double) mt * (double) mt);
+            const double nb = dH < 0.0 ? beta - f / dH : -1.0;
+            if (nb > lo && nb < hi && isfinite(nb)) {
+                beta = nb;
+            } else {
+                fb = 1;
+                beta = isinf(hi) ? 2.0 * beta : 0.5 * (lo + hi);
+            }
+        }
+    }
+    double last_sum = DBL_MIN;
+    int it64 = 0;
+    while (it64 < 200) {
         double sum_P = DBL_MIN, s1 = 0.0, s2 = 0.0;
         for (int m = 0; m < K; ++m) {
             const double e = exp(-beta * d[m]);
+            p[m] = e;
             sum_P += e;
             s1 += d[m] * e;
             s2 += d[m] * d[m] * e;
         }
+        last_sum = sum_P;
         const double Hv = beta * s1 / sum_P + log(sum_P);
-        ++it;
+        ++it64;
         const double f = Hv - logU;
         if (fabs(f) < tol) break;
         if (f > 0.0)
@@ -279,13 +327,9 @@ __global__ void k_calibrate_warm(const double *__restrict__ dist, int stride, in
             beta = isinf(hi) ? 2.0 * beta : 0.5 * (lo + hi);
         }
     }
-    double sum_P = DBL_MIN;
-    for (int m = 0; m < K; ++m) {
-        p[m] = exp(-beta_eval * d[m]);
-        sum_P += p[m];
-    }
-    for (int m = 0; m < K; ++m) p[m] /= sum_P;
-    iters[r] = it;
+    // p holds the last evaluation's row (the accepted one, or the last of 200 steps)
+    for (int m = 0; m < K; ++m) p[m] /= last_sum;
+    iters[r] = it + it64;
     fallback[r] = fb;
 }
 
@@ -486,8 +530,14 @@ int calibrate_rows_learned(const double *dist, int stride, int offset, double *P
 
     // 5. warm-started calibration of the remaining rows
     t0 = now_ms();
-    k_calibrate_warm<<<(nr + 127) / 128, 128, 0, st>>>(dist + (size_t) nh * stride, stride, offset, P + (size_t) nh * K,
-                                                        nr, K, perplexity, beta_hat, iters, fb);
+    int bd = 128;
+    while (bd > 32 && (size_t) bd * K * sizeof(float) > 160 * 1024) bd /= 2;
+    const size_t wsm = (size_t) bd * K * sizeof(float);
+    const int stage = wsm <= 160 * 1024 ? 1 : 0;
+    if (stage) MCK(cudaFuncSetAttribute(k_calibrate_warm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) wsm));
+    k_calibrate_warm<<<(nr + bd - 1) / bd, bd, stage ? wsm : 0, st>>>(dist + (size_t) nh * stride, stride, offset,
+                                                                       P + (size_t) nh * K, nr, K, perplexity,
+                                                                       beta_hat, iters, fb, stage);
     MCK(cudaGetLastError());
     std::vector<int> hi(nr), hf(nr);
     MCK(cudaMemcpyAsync(hi.data(), iters, sizeof(int) * nr, cudaMemcpyDeviceToHost, st));
