@@ -13,11 +13,16 @@ the ~1.56e8 non-zeros of P, gains/momentum/clipping update, zero-mean.
 gb300 arm: P is built on the GPU from the data (exact kNN, calibration, symmetrisation) and
 stays resident; the reference schedule runs untimed from a random start to iteration 300
 (early exaggeration until 250), then W untimed steps, then K steps timed with CUDA events
-on the library's stream (the grid grows from ~50 to ~70 boxes per side over those steps).
+on the library's stream (the grid grows from ~50 to ~100 boxes per side over those steps).
 `e2e` runs the whole pipeline (fitsne_run: data on the host -> embedding on the host, 1000
-iterations of the reference schedule) and reports iterations/s over that wall time.
-The FP64 form of the same kernels is timed on the same steps (`plain_fp64`) and the FP32
-gradient is compared with the FP64 one at the starting state (`grad_rel_l2_vs_fp64`).
+iterations of the reference schedule) with the learned calibration warm start and reports
+iterations/s over that wall time; `e2e.bisection` is the same call with the reference's
+bisection, `e2e.plain_fp64` the FP64 form.  The FP64 form of the same kernels is timed on
+the same steps (`plain_fp64`); the FP32 gradient is compared with the FP64 one at the
+starting state (`grad_rel_l2_vs_fp64`) and with the restated reference gradient (oracle/,
+FP64) on the reference's P at that state (`grad_rel_l2_vs_oracle`).  `on_cpu_inputs` times
+the GPU on exactly the CPU leg's P, start state and steps.  `batch` runs the batched form
+(64 jobs, below) and the same jobs one by one.
 
 reference arm (and the cpu_baseline leg of the gb300 arm, same inputs): the reference's CPU
 path (the C restatement in oracle/, the reference tree is not on the GPU machine) on all host
@@ -25,8 +30,8 @@ cores, on the same step definition; P for that arm is built on the CPU from rand
 within-cluster neighbour lists of the same size (K = 90 per row, symmetrised by the restated
 symmetrizeMatrix): the exact kNN of 1M points on the CPU takes hours.  Y is a synthetic
 post-exaggeration embedding of the same clusters whose grid (60 boxes per side) is the middle
-of the GPU's timed steps.  The number of timed CPU steps is capped so that the arm ends
-within a few minutes.
+of the GPU's timed steps; W untimed steps precede the timed ones.  The number of timed CPU
+steps is capped so that the arm ends within a few minutes.
 
     python bench.py --stage similarities [--n N]
 
@@ -105,14 +110,17 @@ def cpu_sample_P(orc, labels, sizes, K=K_NEIGH, seed=3):
     return r, c, v / v.sum()
 
 
-def time_cpu_steps(orc, P, Y, steps, nthreads, budget_s=None):
-    """Runs reference iterations (post-exaggeration parameters); returns (timed, seconds)."""
+def time_cpu_steps(orc, P, Y, warm, steps, nthreads, budget_s=None):
+    """Runs `warm` untimed reference iterations (post-exaggeration parameters) from Y, then
+    times up to `steps` more, carrying Y, uY and gains through; returns (timed, seconds)."""
     row, col, val = P
     N = Y.shape[0]
     Y = Y.copy()
     uY = np.zeros_like(Y)
     gains = np.ones_like(Y)
     lr = N / 12.0
+    for _ in range(warm):
+        orc.gradient_step(row, col, val, Y, uY, gains, 3, 1.0, 50, nthreads, 1.0, 1.0, 0.8, lr, 1, 5.0)
     done, t0 = 0, time.perf_counter()
     for _ in range(steps):
         orc.gradient_step(row, col, val, Y, uY, gains, 3, 1.0, 50, nthreads, 1.0, 1.0, 0.8, lr, 1, 5.0)
@@ -120,6 +128,18 @@ def time_cpu_steps(orc, P, Y, steps, nthreads, budget_s=None):
         if budget_s is not None and time.perf_counter() - t0 > budget_s:
             break
     return done, time.perf_counter() - t0
+
+
+def reference_P(fitsne, X, perplexity, K):
+    """P as TSNE::run builds it (src/tsne.cpp:153-330): X centred by zeroMean's sequential
+    column sums and scaled by its largest magnitude; exact kNN and calibration (identical to
+    the reference's); symmetrisation; normalisation by the sequential sum."""
+    Xp = X - np.cumsum(X, axis=0)[-1] / len(X)
+    Xp /= np.abs(Xp).max()
+    row, col, val = fitsne.gaussian_perplexity(Xp, perplexity, K)
+    del Xp
+    row, col, val = fitsne.symmetrize(row, col, val, len(X))
+    return row, col, val / np.cumsum(val)[-1]
 
 
 class ClockSampler:
@@ -239,10 +259,11 @@ def run_reference(args, world, rank):
     P = cpu_sample_P(orc, labels, sizes)
     Y = expanded_state(labels)
     cores = os.cpu_count() or 1
-    w_done, w_s = time_cpu_steps(orc, P, Y, args.warmup, cores)
-    per = w_s / max(1, w_done)
+    _, per = time_cpu_steps(orc, P, Y, 0, 1, cores)
     cap = max(1, int(150.0 / max(per, 1e-3)))
-    timed, secs = time_cpu_steps(orc, P, Y, min(args.steps, cap), cores, budget_s=170.0)
+    # W warm-up steps from the synthetic state, then the timed steps (the definition the
+    # GPU arm's on_cpu_inputs leg uses on the same P and state)
+    timed, secs = time_cpu_steps(orc, P, Y, args.warmup, min(args.steps, cap), cores, budget_s=170.0)
     value = timed / secs
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus,
             "steps": args.steps, "steps_timed": timed, "warmup": args.warmup, "ms_per_step": 1e3 * secs / timed,
@@ -250,7 +271,8 @@ def run_reference(args, world, rank):
             "data": "synthetic (seeded Gaussian mixture; random within-cluster P of the same size)",
             "config": config(args, "CPU restatement of the reference path"),
             "cpu_baseline": {"value": value, "unit": "iters/s", "cores": cores, "kind": "port",
-                             "sample": "%d post-exaggeration iterations at N=%d, 2-D" % (timed, args.n)},
+                             "sample": "%d post-exaggeration iterations at N=%d, 2-D, after %d untimed ones from "
+                                       "the synthetic state" % (timed, args.n, args.warmup)},
             "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -315,42 +337,92 @@ def run_gb300(args, world, rank, local):
     abytes = attraction_bytes(N, nnz)
     achieved = abytes / (attr_ms / 1e3) / 1e9
 
-    # end to end: data on the host -> embedding on the host, full schedule
+    # end to end: data on the host -> embedding on the host, full schedule.  The headline
+    # is the FP32 form with the learned calibration warm start; the same call with the
+    # reference's bisection, and the plain FP64 form (bisection) beside it.
     e2e = None
     if not args.skip_e2e:
         rng = np.random.default_rng(1)
         Y0 = rng.standard_normal((N, 2)) * 1e-4
         os.environ.setdefault("FITSNE_QUIET", "1")
-        t2 = time.perf_counter()
-        Yout, costs = fitsne.run(X, Y0=Y0, perplexity=PERPLEXITY, learning_rate=N / 12.0, knn_algo=2, **SCHEDULE)
-        e2e_s = reduce_max(time.perf_counter() - t2, world)
         iters = SCHEDULE["max_iter"]
-        # the plain FP64 form end to end (same kNN, FP64 iterations)
-        fitsne.set_precision(64)
-        try:
-            t3 = time.perf_counter()
-            _, costs64 = fitsne.run(X, Y0=Y0, perplexity=PERPLEXITY, learning_rate=N / 12.0, knn_algo=2, **SCHEDULE)
-            e2e64_s = reduce_max(time.perf_counter() - t3, world)
-        finally:
-            fitsne.set_precision(32)
+
+        def timed_run(calibration, bits):
+            fitsne.set_calibration(calibration)
+            fitsne.set_precision(bits)
+            try:
+                t = time.perf_counter()
+                Yo, c = fitsne.run(X, Y0=Y0, perplexity=PERPLEXITY, learning_rate=N / 12.0, knn_algo=2, **SCHEDULE)
+                secs = reduce_max(time.perf_counter() - t, world)
+                cs = fitsne.calibration_stats()
+            finally:
+                fitsne.set_calibration("bisection")
+                fitsne.set_precision(32)
+            cal_ms = cs["ms_harvest"] + cs["ms_train"] + cs["ms_infer"] + cs["ms_warm"]
+            return Yo, c, secs, cal_ms, cs
+
+        Yout, costs, e2e_s, cal_ms, cs = timed_run("learned", 32)
+        _, costs_b, e2eb_s, calb_ms, csb = timed_run("bisection", 32)
+        _, costs64, e2e64_s, cal64_ms, _ = timed_run("bisection", 64)
         e2e = {"value": world * iters / e2e_s, "unit": "iters/s", "seconds": e2e_s,
                "h2d_bytes_per_step": int((X.nbytes + Y0.nbytes) / iters),
                "d2h_bytes_per_step": int((Yout.nbytes + 16 * iters + 8 * (iters // 50)) / iters),
-               "note": "whole fitsne_run (similarities + %d iterations), bytes averaged per iteration" % iters,
-               "final_kl": float(costs[-1]),
-               "plain_fp64": {"seconds": e2e64_s, "final_kl": float(costs64[-1]), "speedup": e2e64_s / e2e_s}}
+               "note": "whole fitsne_run (similarities with the learned calibration warm start + %d iterations), "
+                       "bytes averaged per iteration" % iters,
+               "final_kl": float(costs[-1]), "calibration_ms": cal_ms,
+               "calibration": {"rows_bisection": cs["rows_harvest"], "evals_per_bisection_row": cs["evals_plain"],
+                               "evals_per_predicted_row": cs["evals_warm"], "train_steps": cs["train_steps"],
+                               "ms_harvest": cs["ms_harvest"], "ms_train": cs["ms_train"],
+                               "ms_infer": cs["ms_infer"], "ms_warm": cs["ms_warm"]},
+               "bisection": {"seconds": e2eb_s, "value": world * iters / e2eb_s, "final_kl": float(costs_b[-1]),
+                             "calibration_ms": calb_ms, "evals_per_row": csb["evals_plain"]},
+               "plain_fp64": {"seconds": e2e64_s, "final_kl": float(costs64[-1]), "calibration_ms": cal64_ms,
+                              "speedup": e2e64_s / e2e_s}}
 
     cpu = None
+    on_cpu_inputs = None
+    grad_vs_oracle = None
     if rank == 0 and not args.skip_cpu:
         import oracle
         oracle.build_restated()
         orc = oracle.Restated()
-        P = cpu_sample_P(orc, labels, sizes)
         cores = os.cpu_count() or 1
-        time_cpu_steps(orc, P, Yst, 1, cores)
-        n, secs = time_cpu_steps(orc, P, Yst, args.cpu_steps, cores)
+        # the FP32 gradient at the bench's starting state against the restated reference
+        # gradient (FP64) on the identical Y and P: the reference's P built as TSNE::run does
+        Pr = reference_P(fitsne, X, PERPLEXITY, K_NEIGH)
+        dg, zg = fitsne.fft_gradient(*Pr, Yburn)
+        dr, zr = orc.fft_gradient(*Pr, Yburn, 3, 1.0, 50, cores, 1.0)
+        grad_vs_oracle = {"rel_l2": float(np.linalg.norm(dg - dr) / np.linalg.norm(dr)),
+                          "z_rel": abs(zg - zr) / zr, "state": "iteration %d of the reference schedule" % STEP_IT0}
+        del Pr, dg, dr
+        # the CPU leg: the restated reference on all host cores
+        P = cpu_sample_P(orc, labels, sizes)
+        n, secs = time_cpu_steps(orc, P, Yst, args.warmup, args.cpu_steps, cores)
         cpu = {"value": n / secs, "unit": "iters/s", "cores": cores, "kind": "port",
-               "sample": "%d post-exaggeration iterations of the restated reference at N=%d, 2-D" % (n, N)}
+               "sample": "%d post-exaggeration iterations of the restated reference at N=%d, 2-D, after %d untimed "
+                         "ones from the synthetic state" % (n, N, args.warmup)}
+        # the GPU on exactly those inputs and steps: P and start state of the CPU leg, the same
+        # untimed steps, then the same number of timed steps (device time of the call)
+        sc = fitsne.Session(*P, Yst, precision=32)
+        try:
+            sc.run(STEP_IT0, STEP_IT0 + args.warmup, **sched)
+            sc.run(STEP_IT0 + args.warmup, STEP_IT0 + args.warmup + n, **sched)
+            ms_a = sc.stage_times()[8]
+            k_long = max(n, 100)
+            sc.run(STEP_IT0 + args.warmup + n, STEP_IT0 + args.warmup + n + k_long, **sched)
+            ms_b = sc.stage_times()[8]
+        finally:
+            sc.close()
+        on_cpu_inputs = {"value": n / (ms_a / 1e3), "unit": "iters/s", "steps": n, "same_inputs": True,
+                         "vs_cpu": (n / (ms_a / 1e3)) / cpu["value"], "nnz": int(P[0][-1]),
+                         "value_next_%d_steps" % k_long: k_long / (ms_b / 1e3),
+                         "note": "P (random within-cluster lists) and start state of the CPU leg, the same %d untimed "
+                                 "steps, then the same %d timed steps (device time)" % (args.warmup, n)}
+        del P
+
+    batch = None
+    if rank == 0 and not args.skip_batch:
+        batch = batch_measure(fitsne, args.jobs)
 
     if rank != 0:
         return 0
@@ -371,6 +443,8 @@ def run_gb300(args, world, rank, local):
             "state_extent": float(np.abs(Yburn).max()),
             "plain_fp64": {"value": fp64_value, "unit": "iters/s", "steps": k64, "speedup": value / fp64_value},
             "grad_rel_l2_vs_fp64": grad_rel, "Z": z32,
+            "grad_rel_l2_vs_oracle": grad_vs_oracle["rel_l2"] if grad_vs_oracle else None,
+            "grad_vs_oracle": grad_vs_oracle, "on_cpu_inputs": on_cpu_inputs, "batch": batch,
             "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e}
     print(json.dumps(line))
     return 0
@@ -448,12 +522,10 @@ def batch_jobs(njobs=64, seed=5):
     return jobs
 
 
-def run_batch(args, world, rank):
-    """The batched form (fitsne_batch_run) against the same jobs run one by one."""
-    if rank != 0:
-        return 0
-    import fitsne
-    jobs = batch_jobs(args.jobs)
+def batch_measure(fitsne, njobs, one_by_one=True):
+    """The batched form (fitsne_batch_run) on the batch_jobs workload, and the same jobs one
+    by one through fitsne_run."""
+    jobs = batch_jobs(njobs)
     Xs = [j[0] for j in jobs]
     perps = [j[1] for j in jobs]
     lrs = [j[2] for j in jobs]
@@ -463,24 +535,36 @@ def run_batch(args, world, rank):
     t0 = time.perf_counter()
     Ys, costs, st = fitsne.batch_run(Xs, perps, learning_rates=lrs, Y0s=Y0s, max_iter=iters)
     batch_s = time.perf_counter() - t0
-    t1 = time.perf_counter()
-    single_kl = []
-    for X, p, lr, Y0 in zip(Xs, perps, lrs, Y0s):
-        _, c = fitsne.run(X, Y0=Y0, perplexity=p, learning_rate=lr, max_iter=iters, knn_algo=2)
-        single_kl.append(c[-1])
-    single_s = time.perf_counter() - t1
-    kl_dev = max(abs(c[-1] - k) / k for c, k in zip(costs, single_kl))
     n = [len(X) for X in Xs]
-    line = {"metric": "batched t-SNE: aggregate iterations/s over %d independent embeddings" % len(jobs),
-            "value": len(jobs) * iters / batch_s, "unit": "iters/s", "n_gpus": 1, "higher_is_better": True,
-            "data": "synthetic (seeded Gaussian mixtures)",
-            "config": {"workload": "%d jobs, N log-uniform in [2000, 50000] (total %d points), D=50, 5-30 clusters, "
-                                   "perplexity 10/30/50 cycled, 2-D, df=1, %d iterations" % (len(jobs), sum(n), iters)},
-            "batch_seconds": batch_s, "similarity_seconds": st["similarity_s"], "iterate_seconds": st["iterate_s"],
-            "iterate_iters_per_s": len(jobs) * iters / st["iterate_s"], "graph_launches": st["graph_launches"],
-            "graph_instantiations": st["graph_instantiations"], "chunks_redone": st["chunks_redone"],
-            "one_by_one_seconds": single_s, "speedup_vs_one_by_one": single_s / batch_s,
-            "max_final_kl_rel_dev_vs_one_by_one": kl_dev}
+    out = {"metric": "batched t-SNE: aggregate iterations/s over %d independent embeddings" % len(jobs),
+           "value": len(jobs) * iters / batch_s, "unit": "iters/s",
+           "workload": "%d jobs, N log-uniform in [2000, 50000] (total %d points), D=50, 5-30 clusters, "
+                       "perplexity 10/30/50 cycled, 2-D, df=1, %d iterations" % (len(jobs), sum(n), iters),
+           "batch_seconds": batch_s, "similarity_seconds": st["similarity_s"], "iterate_seconds": st["iterate_s"],
+           "iterate_iters_per_s": len(jobs) * iters / st["iterate_s"], "graph_launches": st["graph_launches"],
+           "graph_instantiations": st["graph_instantiations"], "chunks_redone": st["chunks_redone"]}
+    if one_by_one:
+        t1 = time.perf_counter()
+        single_kl = []
+        for X, p, lr, Y0 in zip(Xs, perps, lrs, Y0s):
+            _, c = fitsne.run(X, Y0=Y0, perplexity=p, learning_rate=lr, max_iter=iters, knn_algo=2)
+            single_kl.append(c[-1])
+        single_s = time.perf_counter() - t1
+        out.update({"one_by_one_seconds": single_s, "speedup_vs_one_by_one": single_s / batch_s,
+                    "max_final_kl_rel_dev_vs_one_by_one": max(abs(c[-1] - k) / k for c, k in zip(costs, single_kl))})
+    return out
+
+
+def run_batch(args, world, rank):
+    """The batched form (fitsne_batch_run) against the same jobs run one by one."""
+    if rank != 0:
+        return 0
+    import fitsne
+    b = batch_measure(fitsne, args.jobs)
+    line = {"metric": b.pop("metric"), "value": b.pop("value"), "unit": b.pop("unit"), "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic (seeded Gaussian mixtures)",
+            "config": {"workload": b.pop("workload")}}
+    line.update(b)
     print(json.dumps(line))
     return 0
 
@@ -495,6 +579,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--stage", default="iteration", choices=["iteration", "similarities", "batch"])
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--shuffle", action="store_true", help="similarity stage: rows in random order")
