@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "affinity.cuh"
+#include "screen.cuh"
 #include "calib_mlp.cuh"
 #include "knn.cuh"
 #include "sort.cuh"
@@ -79,32 +80,18 @@ __global__ void k_scale(double *__restrict__ X, size_t n, const unsigned long lo
 // FP64 row of the last evaluation, which is always an FP64 one when the bisection
 // converges) are therefore the reference's, bit for bit.
 
-// One bisection step in FP32: +1 when H(beta) - logU > tol for certain, -1 when it is below
-// -tol for certain, 0 when the FP32 value cannot decide.  s[m * sstride] holds the row's
-// distances minus their minimum d0, rounded to FP32.
-//   H = beta sum(d e) / sum(e) + log sum(e) = beta sum(t e') / sum(e') + log sum(e'),
-// with t = d - d0 and e' = exp(-beta t), so both terms are non-negative (sum(e') >= 1) and
-// no cancellation occurs.  Error bound: each e' carries 1.8e-7 |x| + 2.4e-7 relative error
-// (x = -beta t with beta and t rounded to FP32; expf within 2 ulp), the sequential sums
-// K 2^-24 relative; with sum(e') >= 1, |x| e^-|x| <= 1/e and |x|^2 e^-|x| <= 4/e^2 the
-// absolute error of H stays below (3.6e-7 K + 3e-7)(1 + H).  The bound used is
-// (5e-7 K + 2e-6)(1 + H) + 1e-9.  The shifted form is the reference's value only while
-// exp(-beta d0) is far from FP64 underflow, where the
-// reference's DBL_MIN seed of sum_P matters: beyond beta d0 = 600 the step goes to FP64.
+// One bisection step in FP32 (screen_value): +1 when H(beta) - logU > tol for certain, -1
+// when it is below -tol for certain, 0 when the FP32 value cannot decide.  The shifted form
+// is the reference's value only while exp(-beta d0) is far from FP64 underflow, where the
+// reference's DBL_MIN seed of sum_P matters: beyond beta d0 = 600 the step goes to FP64 (and
+// beta must stay within FP32's range).
 __device__ __forceinline__ int screen_step(const float *__restrict__ s, int sstride, int K, double beta, double d0,
                                            double logU, double tol) {
     if (!(beta > 1e-30 && beta < 1e30) || beta * d0 > 600.0) return 0;
-    const float bf = (float) beta;
-    float B = 0.f, A = 0.f;
-    for (int m = 0; m < K; ++m) {
-        const float t = s[(size_t) m * sstride];
-        const float e = expf(-bf * t);
-        B += e;
-        A = fmaf(t, e, A);
-    }
-    const float h = bf * (A / B) + logf(B);
-    const double E = (5e-7 * K + 2e-6) * (1.0 + fabs((double) h)) + 1e-9;
+    double E;
+    const float h = screen_value(s, sstride, K, beta, &E);
     const double Hd = (double) h - logU;
+    if (!(E < 1e-2)) return 0;
     if (Hd > tol + E) return 1;
     if (Hd < -(tol + E)) return -1;
     return 0;

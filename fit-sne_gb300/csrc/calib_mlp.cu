@@ -13,13 +13,14 @@
 
 #include "affinity.cuh"
 #include "calib_mlp.cuh"
+#include "screen.cuh"
 
 namespace fitsne {
 namespace {
 
 constexpr int H = kMlpHidden;
 constexpr int kSPB = 8;          // samples per block in the gradient kernel
-constexpr int kBatch = 256;      // minibatch
+constexpr int kBatch = 512;      // minibatch (FITSNE_MLP_BATCH overrides)
 constexpr int kGraphSteps = 25;  // optimiser steps per captured graph
 constexpr float kLr = 2e-3f;     // Adam step size
 constexpr int kH2 = H + 1;       // padded row stride of W2 in shared memory
@@ -238,9 +239,9 @@ size_t infer_smem(int K) {
 //
 // The first steps run in FP32 on the row's distances shifted by their minimum (staged in
 // shared memory, one column per thread), where H = beta <t> + log sum exp(-beta t) has no
-// cancellation and a bound on its error (the one of the bisection's FP32 screen): a step
+// cancellation and a bound on its error (screen_value, shared with the bisection): a step
 // moves the bracket only when the sign of H - log U is certain, and the FP32 phase ends when
-// |H - log U| is within that bound.  The FP64 steps that follow take the row to the
+// |H - log U| is within that bound, after one last Newton step from that value.  The FP64 steps that follow take the row to the
 // acceptance test |H - log U| < 1e-6; each writes exp(-beta d) to the output row, so the
 // accepted evaluation's values only need the normalisation.
 __global__ void k_calibrate_warm(const double *__restrict__ dist, int stride, int offset, double *__restrict__ P,
@@ -268,33 +269,30 @@ __global__ void k_calibrate_warm(const double *__restrict__ dist, int stride, in
         const size_t sst = blockDim.x;
         for (int m = 0; m < K; ++m) w[m * sst] = (float) (d[m] - d0);
         while (it < 30 && beta > 1e-30 && beta < 1e30 && beta * d0 <= 600.0) {
-            const float bf = (float) beta;
-            float B = 0.f, A1 = 0.f, A2 = 0.f;
-            for (int m = 0; m < K; ++m) {
-                const float t = w[m * sst];
-                const float e = expf(-bf * t);
-                B += e;
-                A1 = fmaf(t, e, A1);
-                A2 = fmaf(t * t, e, A2);
-            }
+            double E;
+            float mt, m2;
+            const float h = screen_value(w, (int) sst, K, beta, &E, &mt, &m2);
             ++it;
-            const float mt = A1 / B;
-            const float h = bf * mt + logf(B);
             const double f = (double) h - logU;
-            const double E = (5e-7 * K + 2e-6) * (1.0 + fabs((double) h)) + 1e-9;
-            if (fabs(f) <= E + tol) break;  // FP32 cannot resolve further: FP64 from here
-            if (f > 0.0)
-                lo = beta;
-            else
-                hi = beta;
-            const double dH = -beta * ((double) (A2 / B) - (double) mt * (double) mt);
+            const bool last = !(fabs(f) > E + tol) || !(E < 1e-2);
+            if (!last) {  // the sign is certain: the bracket moves
+                if (f > 0.0)
+                    lo = beta;
+                else
+                    hi = beta;
+            }
+            // dH/dbeta = -beta Var(t) (the variance is shift-invariant)
+            const double dH = -beta * ((double) m2 - (double) mt * (double) mt);
             const double nb = dH < 0.0 ? beta - f / dH : -1.0;
             if (nb > lo && nb < hi && isfinite(nb)) {
                 beta = nb;
-            } else {
+            } else if (!last) {
                 fb = 1;
                 beta = isinf(hi) ? 2.0 * beta : 0.5 * (lo + hi);
             }
+            // within the FP32 value's error bound of the target: one last Newton step from it
+            // (taken above when it stays in the bracket), then FP64 from here
+            if (last) break;
         }
     }
     double last_sum = DBL_MIN;
@@ -480,19 +478,24 @@ int calibrate_rows_learned(const double *dist, int stride, int offset, double *P
     MCK(cudaMemsetAsync(v, 0, sizeof(float) * o.n, st));
     MCK(cudaMemsetAsync(loss, 0, sizeof(double), st));
     MCK(cudaMemsetAsync(step, 0, sizeof(unsigned), st));
-    // 1200 steps of 256: the search only needs a seed within a few per cent of beta
-    const int nsteps = 1200 / kGraphSteps * kGraphSteps;
+    // 300 steps of 512 rows (FITSNE_MLP_STEPS / FITSNE_MLP_BATCH override): the search only
+    // needs a seed within a few per cent of beta; its FP32 Newton steps correct the rest at
+    // little cost, and the FP64 evaluations it needs do not depend on the seed's accuracy
+    int batch = kBatch, want = 300;
+    if (const char *eb = std::getenv("FITSNE_MLP_BATCH")) batch = std::max(kSPB, std::min(8192, std::atoi(eb)));
+    if (const char *es = std::getenv("FITSNE_MLP_STEPS")) want = std::max(kGraphSteps, std::min(20000, std::atoi(es)));
+    const int nsteps = want / kGraphSteps * kGraphSteps;
     MCK(b.get(&hist, (size_t) nsteps));
     const size_t gsm = grad_smem(K);
     MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) gsm));
-    const int gblocks = (kBatch + kSPB - 1) / kSPB;
+    const int gblocks = (batch + kSPB - 1) / kSPB;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     MCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < kGraphSteps; ++k) {
-        k_mlp_grad<<<gblocks, H, gsm, st>>>(params, K, x, target, nh, kBatch, (float) mu, (float) (1.0 / sd), step,
+        k_mlp_grad<<<gblocks, H, gsm, st>>>(params, K, x, target, nh, batch, (float) mu, (float) (1.0 / sd), step,
                                             grad, loss);
-        k_adam<<<1, 1024, 0, st>>>(params, grad, m, v, o.n, step, loss, hist, kBatch);
+        k_adam<<<1, 1024, 0, st>>>(params, grad, m, v, o.n, step, loss, hist, batch);
     }
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
     if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
