@@ -67,10 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(lib_srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda s: _compile(s, force), lib_srcs))
     if force or _stale(LIB, objs):
-        # cuBLAS serves the PCA initialisation's plain FP64 GEMMs; rpath to the toolkit's lib64
-        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(_nvcc()))), "lib64")
-        cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + [
-            "-lcublas", "-Xlinker", "-rpath=" + cuda_lib, "-lpthread"]
+        cmd = [_nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))
