@@ -112,6 +112,40 @@ def test_affinity_files_save_and_load(gpu_lib, golden, tmp_path, monkeypatch):
     assert abs(ca[49] - cb[49]) <= 1e-2 * ca[49]
 
 
+def test_p_files_interchange_with_the_reference(gpu_lib, golden, tmp_path, monkeypatch):
+    """P files of the compiled reference (load_affinities = 2, src/tsne.cpp:333-366;
+    tests/golden/pfiles_e2e.npz) against fitsne_run's.  The files fitsne_run writes have the
+    reference's rows and columns byte for byte, and its values within 1e-13 relative: the
+    GPU's exp and the host's may differ in the last bit, and the normalisation divides by the
+    sum of P, which the reference adds up sequentially and the GPU by a parallel reduction
+    (measured: within 3e-14).  The reference's files load with load_affinities = 1
+    (src/tsne.cpp:236-281) and the FP64 form then follows the reference's run on that P to
+    rounding level at the first checkpoint."""
+    pf = np.load(os.path.join(os.path.dirname(__file__), "golden", "pfiles_e2e.npz"))
+    monkeypatch.chdir(tmp_path)
+    X, Y0 = golden["e2e_X"], golden["e2e_Y0"]
+    kw = dict(Y0=Y0, perplexity=15.0, stop_lying_iter=100, mom_switch_iter=100, learning_rate=200.0, knn_algo=2)
+    gpu_lib.run(X, load_affinities=2, max_iter=1, **kw)
+    row = np.fromfile("P_row.dat", np.uint32)
+    col = np.fromfile("P_col.dat", np.uint32)
+    val = np.fromfile("P_val.dat", np.float64)
+    assert np.array_equal(row, pf["P_row"]) and np.array_equal(col, pf["P_col"])
+    assert np.allclose(val, pf["P_val"], rtol=1e-13, atol=0)
+    # the reference's files, loaded
+    pf["P_row"].tofile("P_row.dat")
+    pf["P_col"].tofile("P_col.dat")
+    pf["P_val"].tofile("P_val.dat")
+    gpu_lib.set_precision(64)
+    try:
+        Y, costs = gpu_lib.run(X, load_affinities=1, max_iter=300, **kw)
+    finally:
+        gpu_lib.set_precision(32)
+    ref = golden["e2e_costs"]
+    assert abs(costs[49] - ref[49]) <= 1e-8 * ref[49], (costs[49], ref[49])
+    assert abs(costs[299] - ref[299]) <= 3e-2 * ref[299]
+    assert np.isfinite(Y).all()
+
+
 def _kl5000():
     import make_kl_5000 as m
     return m, np.load(os.path.join(os.path.dirname(__file__), "golden", "kl_5000.npz"))
