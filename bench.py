@@ -327,6 +327,7 @@ def run_gb300(args, world, rank, local):
         wall = time.perf_counter() - t1
     run_ms = reduce_max(s32.stage_times()[8], world)
     launches = int(s32.stage_times()[9])
+    shapes = s32.launch_shapes()
     s32.set_timing(True)
     k_st = max(10, min(args.steps, 60))
     s32.run(it_b, it_b + k_st, **sched)
@@ -439,7 +440,7 @@ def run_gb300(args, world, rank, local):
                          "note": "per-stage CUDA events over %d further steps on the host path (one min/max round "
                                  "trip per iteration, inside the spread stage); value and ms_per_step are the "
                                  "graph-captured production path" % k_st},
-            "nnz": nnz, "wall_ms_per_step": 1e3 * wall / args.steps, "setup_s": setup_s,
+            "launch_shapes": shapes, "nnz": nnz, "wall_ms_per_step": 1e3 * wall / args.steps, "setup_s": setup_s,
             "state_extent": float(np.abs(Yburn).max()),
             "plain_fp64": {"value": fp64_value, "unit": "iters/s", "steps": k64, "speedup": value / fp64_value},
             "grad_rel_l2_vs_fp64": grad_rel, "Z": z32,

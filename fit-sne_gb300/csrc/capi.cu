@@ -217,6 +217,12 @@ int fitsne_session_stage_times(fitsne_session *s, double *out10) {
     return 0;
 }
 
+int fitsne_session_launch_shapes(fitsne_session *s, int *out5) {
+    if (!s || !s->impl || !out5) return set_error(FITSNE_E_ARG, "null argument");
+    s->impl->launch_shapes(out5);
+    return 0;
+}
+
 void fitsne_session_destroy(fitsne_session *s) {
     if (!s) return;
     cudaStream_t st = s->impl ? s->impl->st : nullptr;

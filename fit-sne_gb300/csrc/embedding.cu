@@ -198,21 +198,111 @@ int Embedding<T>::prepare_grid() {
         }
         L_ = L;
     }
+    if (!twiddles(L)) return -10;
+    int rc = grid_buffers(M, L);
+    if (!rc && fft_thr_L_ != L) rc = tune_fft(M, L);
+    return rc;
+}
+
+template <typename T>
+typename Embedding<T>::C *Embedding<T>::twiddles(int L) {
     auto it = tw_.find(L);
-    if (it == tw_.end()) {
-        std::vector<C> h(L);
-        const double pi = 3.14159265358979323846264338327950288;
-        for (int j = 0; j < L; ++j) {
-            const double a = 2.0 * pi * (double) j / (double) L;
-            h[j] = mkc((T) std::cos(a), (T) -std::sin(a));
-        }
-        C *d = nullptr;
-        FITSNE_CK(cudaMalloc(&d, sizeof(C) * L));
-        FITSNE_CK(cudaMemcpyAsync(d, h.data(), sizeof(C) * L, cudaMemcpyHostToDevice, st_));
-        FITSNE_CK(cudaStreamSynchronize(st_));
-        tw_[L] = d;
+    if (it != tw_.end()) return it->second;
+    std::vector<C> h(L);
+    const double pi = 3.14159265358979323846264338327950288;
+    for (int j = 0; j < L; ++j) {
+        const double a = 2.0 * pi * (double) j / (double) L;
+        h[j] = mkc((T) std::cos(a), (T) -std::sin(a));
     }
-    return grid_buffers(M, L);
+    C *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(C) * L);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, h.data(), sizeof(C) * L, cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) {
+        fail("twiddles", e);
+        cudaFree(d);
+        return nullptr;
+    }
+    tw_[L] = d;
+    return d;
+}
+
+// Threads per block of the five 2-D FFT passes (kFftThreadChoices), timed on this
+// embedding's grid buffers at transform length L the first time L occurs in the process
+// (FITSNE_FFT_THREADS fixes it; FITSNE_AUTOTUNE=0 keeps 256).  Smaller blocks put more
+// blocks on an SM for the short transforms of small grids; larger ones share each
+// transform's stages among more threads.
+template <typename T>
+int Embedding<T>::tune_fft(int M, int L) {
+    fft_thr_L_ = L;
+    fft_thr_ = 256;
+    if (D_ != 2) return 0;
+    const char *fx = std::getenv("FITSNE_FFT_THREADS");
+    if (fx && *fx) {
+        fft_thr_ = std::atoi(fx);
+        return 0;
+    }
+    const char *e = std::getenv("FITSNE_AUTOTUNE");
+    if (e && std::atoi(e) == 0) return 0;
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, int> chosen;
+    const std::pair<int, int> key((int) sizeof(T), L);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = chosen.find(key);
+        if (it != chosen.end()) {
+            fft_thr_ = it->second;
+            return 0;
+        }
+    }
+    FftPlan pl;
+    if (!make_fft_plan(L, &pl)) return 0;
+    C *tw = twiddles(L);
+    if (!tw) return -10;
+    const int mode = (gp_.df == 1.0) ? KERNEL_DF1 : KERNEL_VARDF;
+    cudaEvent_t a = nullptr, b = nullptr;
+    FITSNE_CK(cudaEventCreate(&a));
+    FITSNE_CK(cudaEventCreate(&b));
+    int best = 256;
+    float best_ms = 0.f;
+    for (int ci = 0; ci < 3; ++ci) {
+        const int thr = kFftThreadChoices[(ci + 1) % 3];  // 256 first
+        FITSNE_CK(conv2d_launch<T>(grid_in_, grid_out_, M, pl, tw, work_a_, work_b_, kspec_, 0.05, gp_.df, mode,
+                                   st_, thr));
+        FITSNE_CK(cudaEventRecord(a, st_));
+        for (int r = 0; r < 3; ++r)
+            FITSNE_CK(conv2d_launch<T>(grid_in_, grid_out_, M, pl, tw, work_a_, work_b_, kspec_, 0.05, gp_.df, mode,
+                                       st_, thr));
+        FITSNE_CK(cudaEventRecord(b, st_));
+        FITSNE_CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (timing_requested()) std::fprintf(stderr, "[fitsne] FFT passes, L = %d, %d threads: %.4f ms\n", L, thr, ms / 3.f);
+        if (ci == 0 || ms < 0.97f * best_ms) {
+            best = thr;
+            best_ms = ms;
+        }
+    }
+    launches_ += 4 * 3 * 5;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        chosen[key] = best;
+    }
+    fft_thr_ = best;
+    return 0;
+}
+
+template <typename T>
+void Embedding<T>::launch_shapes(int *out5) const {
+    int g = 0, u = 0;
+    attr_shape_info(attr_shape_, &g, &u);
+    out5[0] = attr_shape_;
+    out5[1] = g;
+    out5[2] = u;
+    out5[3] = 0;
+    out5[4] = fft_thr_;
 }
 
 template <typename T>
@@ -258,7 +348,7 @@ int Embedding<T>::repulsion() {
     if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][2], st_));
     if (D_ == 2)
         FITSNE_CK(conv2d_launch<T>(grid_in_, grid_out_, M, plan_, tw_[L_], work_a_, work_b_, kspec_, geom_.hk,
-                                   gp_.df, mode, st_));
+                                   gp_.df, mode, st_, fft_thr_));
     else
         FITSNE_CK(conv1d_launch<T>(grid_in_, grid_out_, M, plan_, tw_[L_], work_a_, geom_.hk, gp_.df, mode, st_));
     if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][3], st_));
@@ -675,6 +765,10 @@ int Embedding<T>::plan_capacity(int grow) {
     }
     int rc = grid_buffers(M, L);
     if (rc) return rc;
+    if (fft_thr_L_ != L) {
+        rc = tune_fft(M, L);
+        if (rc) return rc;
+    }
     if (L > tw_dev_cap_) {
         cudaFree(tw_dev_);
         FITSNE_CK(cudaMalloc(&tw_dev_, sizeof(C) * L));
@@ -717,7 +811,7 @@ int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_f
         FITSNE_CK(launch_spread_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_in_, st_));
         if (D_ == 2)
             FITSNE_CK(conv2d_launch_dev<T>(grid_in_, grid_out_, M_cap_, L_cap_, cg, tw_dev_, work_a_, work_b_, kspec_,
-                                           gp_.df, mode, st_));
+                                           gp_.df, mode, st_, fft_thr_));
         else
             FITSNE_CK(conv1d_launch_dev<T>(grid_in_, grid_out_, L_cap_, cg, tw_dev_, work_a_, gp_.df, mode, st_));
         FITSNE_CK(launch_gather_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_out_, mode, rep_, red_, st_, yh_));
@@ -824,6 +918,7 @@ std::vector<unsigned long long> Embedding<T>::chunk_key(const UpdateParams &p, i
     put(&nb_cap_, sizeof nb_cap_);
     put(&excl_, sizeof excl_);
     put(&attr_shape_, sizeof attr_shape_);
+    put(&fft_thr_, sizeof fft_thr_);
     for (const void *q : {(const void *) row_, (const void *) col_, (const void *) val_, (const void *) Y_[0],
                           (const void *) Y_[1], (const void *) uY_, (const void *) gains_, (const void *) rep_,
                           (const void *) grid_in_, (const void *) grid_out_, (const void *) work_a_,

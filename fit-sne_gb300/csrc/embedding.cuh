@@ -130,6 +130,10 @@ class Embedding {
     int N() const { return N_; }
     cudaStream_t stream() const { return st_; }
     const std::string &error() const { return err_; }
+    // launch shapes in use: attraction shape index, its rows per work item (points per tile
+    // block in the tiled form) and edges per lane, the attraction's form (0 full CSR, 2 tiled),
+    // FFT threads per block
+    void launch_shapes(int *out5) const;
     // device pointers (for zero-copy consumers such as the no-allocation path)
     const uint32_t *d_row() const { return row_; }
     const uint32_t *d_col() const { return col_; }
@@ -187,6 +191,10 @@ class Embedding {
     int attr_phase_ = -1;  // tune_phase_ that attr_shape_ was chosen for
     int tune_phase_ = 1;   // phase of the current iteration (tune_phase)
     int tune_attr(bool measure);
+    // autotuned threads per block of the 2-D FFT passes, per transform length (fft_thr_L_)
+    int fft_thr_ = 256, fft_thr_L_ = 0;
+    int tune_fft(int M, int L);
+    C *twiddles(int L);  // host-built twiddles of length L (cached in tw_)
     // graph chunks
     bool graphs_ = true;
     DevGeom *dgeom_ = nullptr;         // device: geometry of the current iteration

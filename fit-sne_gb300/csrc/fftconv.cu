@@ -543,7 +543,7 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 template <typename T>
 cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, const FftPlan &plan,
                           const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
-                          KSpec<T> *kspec, double h, double df, int mode, cudaStream_t st) {
+                          KSpec<T> *kspec, double h, double df, int mode, cudaStream_t st, int threads) {
     typedef typename Cx<T>::t C;
     const int L = plan.L, H = L / 2 + 1;
     if (L > max_fft_len<T>() || L < 2 * M) return cudaErrorInvalidValue;
@@ -555,7 +555,7 @@ cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
     if ((e = set_smem(k_data_rows<T>, s4)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_cols<T>, s5)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
-    const int thr = 256;
+    const int thr = (threads >= 32 && threads <= 1024 && threads % 32 == 0) ? threads : 256;
     // kernel spectra: krow uses work_a ([4][L][H]); data passes use work_b ([4][M][H]) then work_a
     k_kernel_rows<T><<<M, thr, s4, st>>>(M, plan, tw, work_a, (T) h, (T) df, mode, nullptr);
     k_kernel_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_a, kspec, nullptr);
@@ -568,7 +568,7 @@ cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
 template <typename T>
 cudaError_t conv2d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M_cap, int L_cap, const ConvGeom *cg,
                               const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
-                              KSpec<T> *kspec, double df, int mode, cudaStream_t st) {
+                              KSpec<T> *kspec, double df, int mode, cudaStream_t st, int threads) {
     typedef typename Cx<T>::t C;
     const int H = L_cap / 2 + 1;
     if (L_cap > max_fft_len<T>() || L_cap < 2 * M_cap) return cudaErrorInvalidValue;
@@ -580,7 +580,7 @@ cudaError_t conv2d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M
     if ((e = set_smem(k_data_rows<T>, s4)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_cols<T>, s5)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
-    const int thr = 256;
+    const int thr = (threads >= 32 && threads <= 1024 && threads % 32 == 0) ? threads : 256;
     FftPlan dummy{};
     k_kernel_rows<T><<<M_cap, thr, s4, st>>>(0, dummy, tw, work_a, T(0), (T) df, mode, cg);
     k_kernel_cols<T><<<H, thr, s5, st>>>(0, dummy, tw, work_a, kspec, cg);
@@ -756,20 +756,20 @@ template cudaError_t conv2d_launch_batch<float>(const Cell4<float> *, Cell4<floa
 template cudaError_t twiddles_batch<float>(const FftBatchJob *, int, float2 *, cudaStream_t);
 
 template cudaError_t conv2d_launch<float>(const Cell4<float> *, Cell4<float> *, int, const FftPlan &, const float2 *,
-                                          float2 *, float2 *, KSpec<float> *, double, double, int, cudaStream_t);
+                                          float2 *, float2 *, KSpec<float> *, double, double, int, cudaStream_t, int);
 template cudaError_t conv2d_launch<double>(const Cell4<double> *, Cell4<double> *, int, const FftPlan &,
                                            const double2 *, double2 *, double2 *, KSpec<double> *, double, double,
-                                           int, cudaStream_t);
+                                           int, cudaStream_t, int);
 template cudaError_t conv1d_launch<float>(const Cell4<float> *, Cell4<float> *, int, const FftPlan &, const float2 *,
                                           float2 *, double, double, int, cudaStream_t);
 template cudaError_t conv1d_launch<double>(const Cell4<double> *, Cell4<double> *, int, const FftPlan &,
                                            const double2 *, double2 *, double, double, int, cudaStream_t);
 template cudaError_t conv2d_launch_dev<float>(const Cell4<float> *, Cell4<float> *, int, int, const ConvGeom *,
                                               const float2 *, float2 *, float2 *, KSpec<float> *, double, int,
-                                              cudaStream_t);
+                                              cudaStream_t, int);
 template cudaError_t conv2d_launch_dev<double>(const Cell4<double> *, Cell4<double> *, int, int, const ConvGeom *,
                                                const double2 *, double2 *, double2 *, KSpec<double> *, double, int,
-                                               cudaStream_t);
+                                               cudaStream_t, int);
 template cudaError_t conv1d_launch_dev<float>(const Cell4<float> *, Cell4<float> *, int, const ConvGeom *,
                                               const float2 *, float2 *, double, int, cudaStream_t);
 template cudaError_t conv1d_launch_dev<double>(const Cell4<double> *, Cell4<double> *, int, const ConvGeom *,

@@ -86,7 +86,7 @@ enum KernelMode { KERNEL_DF1 = 0, KERNEL_VARDF = 1 };
 template <typename T>
 cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, const FftPlan &plan,
                           const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
-                          KSpec<T> *kspec, double h, double df, int mode, cudaStream_t st);
+                          KSpec<T> *kspec, double h, double df, int mode, cudaStream_t st, int threads = 256);
 
 // As conv2d_launch with the geometry read from device memory (cg); grids and shared
 // memory sized for M_cap and L_cap (cg->M <= M_cap, cg->plan.L <= L_cap; tw holds the
@@ -94,7 +94,10 @@ cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
 template <typename T>
 cudaError_t conv2d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M_cap, int L_cap, const ConvGeom *cg,
                               const typename Cx<T>::t *tw, typename Cx<T>::t *work_a, typename Cx<T>::t *work_b,
-                              KSpec<T> *kspec, double df, int mode, cudaStream_t st);
+                              KSpec<T> *kspec, double df, int mode, cudaStream_t st, int threads = 256);
+// Threads per block the 2-D passes accept (any multiple of 32 up to 1024); the launch shapes
+// the autotuner picks from.
+constexpr int kFftThreadChoices[3] = {128, 256, 512};
 template <typename T>
 cudaError_t conv1d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int L_cap, const ConvGeom *cg,
                               const typename Cx<T>::t *tw, typename Cx<T>::t *work, double df, int mode,

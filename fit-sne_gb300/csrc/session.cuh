@@ -16,6 +16,7 @@ struct SessionBase {
     virtual void set_timing(bool on) = 0;
     virtual void set_graphs(bool on) = 0;
     virtual void times(double *out10) = 0;
+    virtual void launch_shapes(int *out5) = 0;
     virtual std::string error() = 0;
     cudaStream_t st = nullptr;
 };
@@ -43,6 +44,7 @@ struct SessionT : SessionBase {
         o[8] = t.run_ms;
         o[9] = (double) t.launches;
     }
+    void launch_shapes(int *o) override { emb.launch_shapes(o); }
     std::string error() override { return emb.error(); }
 };
 

@@ -64,6 +64,7 @@ _SIGS = {
     "fitsne_session_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fitsne_session_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fitsne_session_stage_times": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
+    "fitsne_session_launch_shapes": (ctypes.c_int, [ctypes.c_void_p, _i32p]),
     "fitsne_session_destroy": (None, [ctypes.c_void_p]),
     "fitsne_fft_gradient_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                    ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
@@ -419,6 +420,14 @@ class Session:
         out = np.zeros(10)
         _check(lib().fitsne_session_stage_times(self._h, _p(out, _f64p)))
         return out
+
+    def launch_shapes(self):
+        """The autotuner's choices: attraction shape index, rows per work item, edges per lane,
+        attraction form (0 full CSR, 2 tiled), FFT threads per block."""
+        out = np.zeros(5, np.int32)
+        _check(lib().fitsne_session_launch_shapes(self._h, _p(out, _i32p)))
+        keys = ["attr_shape", "attr_rows_per_item", "attr_edges_per_lane", "attr_form", "fft_threads"]
+        return dict(zip(keys, [int(v) for v in out]))
 
     def close(self):
         if getattr(self, "_h", None):

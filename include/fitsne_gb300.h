@@ -150,6 +150,12 @@ int fitsne_session_set_timing(fitsne_session *s, int on);
  * sized on the device; 0: one host round trip per iteration (the per-stage timing path). */
 int fitsne_session_set_graphs(fitsne_session *s, int on);
 int fitsne_session_stage_times(fitsne_session *s, double *out10);
+/* Launch shapes the session's autotuner chose (no reference counterpart), out[5]: the
+ * attraction's shape index (FITSNE_ATTR_SHAPE numbering; -1 before the first choice), its rows
+ * per work item (points per block in the tiled form) and edges per lane, its form (0 over the
+ * full CSR, 2 tiled over the half-stored symmetric P), and the threads per block of the 2-D FFT
+ * passes. */
+int fitsne_session_launch_shapes(fitsne_session *s, int *out5);
 void fitsne_session_destroy(fitsne_session *s);
 
 /* ---------------------------------------------------------------------------------

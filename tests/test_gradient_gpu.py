@@ -145,3 +145,22 @@ def test_every_attraction_shape_takes_the_same_steps(gpu_lib, monkeypatch, bits)
         gpu_lib.set_precision(32)
     for shape in range(1, N_SHAPES):
         assert rel_l2(out[shape], out[0]) < (1e-4 if bits == 32 else 1e-9), shape
+
+
+@pytest.mark.parametrize("threads", [64, 128, 512])
+@pytest.mark.parametrize("bits", [32, 64])
+def test_every_fft_block_size_gives_the_reference_gradient(gpu_lib, golden, monkeypatch, bits, threads):
+    """The 2-D FFT passes accept any block size the autotuner may pick (FITSNE_FFT_THREADS
+    fixes it): the same gradient within the FP32 / FP64 tolerances, on the default grid and on
+    the finer nterms = 5 fixture."""
+    monkeypatch.setenv("FITSNE_FFT_THREADS", str(threads))
+    row, col, val = _P(golden)
+    gpu_lib.set_precision(bits)
+    try:
+        dC, z = gpu_lib.fft_gradient(row, col, val, golden["Y2"], 3, 1.0, 50, 1.0)
+        dC5, z5 = gpu_lib.fft_gradient(row, col, val, golden["Y2"], 5, 2.0, 30, 1.0)
+    finally:
+        gpu_lib.set_precision(32)
+    assert rel_l2(dC, golden["g2_df1_dC"]) < TOL[bits][0]
+    assert abs(z - float(golden["g2_df1_Z"])) < TOL[bits][1] * float(golden["g2_df1_Z"])
+    assert rel_l2(dC5, golden["g2_nt5_dC"]) < TOL[bits][0]
