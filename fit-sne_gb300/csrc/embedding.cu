@@ -52,6 +52,10 @@ Embedding<T>::~Embedding() {
         cudaFree(p);
     cudaFree(red_mem_);
     cudaFree(red_cnt_);
+    cudaFree(urow_);
+    cudaFree(trec_);
+    cudaFree(tstart_);
+    cudaFree(acc_);
     if (h_pin_) cudaFreeHost(h_pin_);
     cudaFree(dgeom_);
     cudaFree(gstatus_);
@@ -145,7 +149,7 @@ int Embedding<T>::init_host(int N, int D, const uint32_t *row, const uint32_t *c
     cudaFree(tmp);
     cur_ = 0;
     mean_pending_ = false;
-    return 0;
+    return check_symmetric();
 }
 
 template <typename T>
@@ -168,7 +172,116 @@ int Embedding<T>::init_device(int N, int D, const uint32_t *d_row, const uint32_
     cudaFree(tmp);
     cur_ = 0;
     mean_pending_ = false;
+    return check_symmetric();
+}
+
+// The tiled attraction needs P symmetric in pattern and values (symmetrizeMatrix's output
+// is; a caller's P need not be): checked once by hashing the entries and their transposes on
+// the device.  A renumbering keeps the symmetry.
+template <typename T>
+int Embedding<T>::check_symmetric() {
+    sym_ok_ = false;
+    tiles_ok_ = false;
+    if (sizeof(T) != 4 || nnz_ == 0) return 0;
+    const char *e = std::getenv("FITSNE_ATTR_SYM");
+    if (e && std::atoi(e) == 0) return 0;
+    unsigned long long *h = nullptr;
+    FITSNE_CK(cudaMalloc(&h, 2 * sizeof(unsigned long long)));
+    FITSNE_CK(launch_sym_hash(row_, col_, reinterpret_cast<const float *>(val_), N_, h, st_));
+    unsigned long long hh[2] = {0, 1};
+    FITSNE_CK(cudaMemcpyAsync(hh, h, sizeof hh, cudaMemcpyDeviceToHost, st_));
+    FITSNE_CK(cudaStreamSynchronize(st_));
+    cudaFree(h);
+    if (hh[0] != hh[1]) return 0;
+    sym_ok_ = true;
+    return build_tiles();
+}
+
+// Records of the upper entries sorted by tile (A, B) of 4,096-point blocks, row order kept
+// within a tile (stable radix sort on the tile key), and the tiles' first records.  Rebuilt
+// after every renumbering: the tiles follow the point order.
+template <typename T>
+int Embedding<T>::build_tiles() {
+    tiles_ok_ = false;
+    if (!sym_ok_) return 0;
+    const int nblk = tile_blocks(N_);
+    const size_t nkeys = (size_t) nblk * nblk;
+    if (nkeys >= (1ull << 30)) return 0;
+    int key_bits = 1;
+    while (((size_t) 1 << key_bits) < nkeys) ++key_bits;
+    uint32_t *ulen = nullptr, *keys = nullptr, *ids = nullptr, *keys2 = nullptr, *ids2 = nullptr, *tcount = nullptr;
+    uint2 *rec = nullptr;
+    void *scr = nullptr;
+    auto release = [&]() {
+        cudaFree(ulen);
+        cudaFree(keys);
+        cudaFree(ids);
+        cudaFree(keys2);
+        cudaFree(ids2);
+        cudaFree(tcount);
+        cudaFree(rec);
+        cudaFree(scr);
+    };
+    cudaError_t e = cudaSuccess;
+    if (!urow_) e = cudaMalloc(&urow_, sizeof(uint32_t) * (N_ + 1));
+    if (e == cudaSuccess && !acc_) {
+        e = cudaMalloc(&acc_, sizeof(float) * (size_t) N_ * D_);
+        if (e == cudaSuccess) e = cudaMemsetAsync(acc_, 0, sizeof(float) * (size_t) N_ * D_, st_);
+    }
+    // upper entries per row and their row offsets
+    if (e == cudaSuccess) e = cudaMalloc(&ulen, sizeof(uint32_t) * (N_ + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&scr, std::max(scan_scratch_bytes((size_t) N_ + 1), scan_scratch_bytes(nkeys + 1)));
+    if (e == cudaSuccess) e = launch_upper_count(row_, col_, N_, ulen, st_);
+    if (e == cudaSuccess) e = exclusive_scan_u32(ulen, urow_, (size_t) N_, scr, st_);
+    unsigned int total = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, urow_ + N_, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    const size_t n = total;
+    if (e == cudaSuccess && n > 0) {
+        cudaFree(scr);
+        scr = nullptr;
+        const size_t scr_bytes = std::max(radix_sort_scratch_bytes(n), scan_scratch_bytes(nkeys + 1));
+        for (auto pr : {std::make_pair((void **) &keys, n * 4), std::make_pair((void **) &ids, n * 4),
+                        std::make_pair((void **) &keys2, n * 4), std::make_pair((void **) &ids2, n * 4),
+                        std::make_pair((void **) &tcount, nkeys * 4), std::make_pair((void **) &rec, n * 8),
+                        std::make_pair((void **) &scr, scr_bytes)})
+            if (e == cudaSuccess) e = cudaMalloc(pr.first, pr.second);
+        if (e == cudaSuccess && (!trec_ || n > unnz_)) {
+            cudaFree(trec_);
+            trec_ = nullptr;
+            e = cudaMalloc(&trec_, sizeof(uint2) * n);
+            unnz_ = n;
+        }
+        if (e == cudaSuccess) {
+            cudaFree(tstart_);
+            tstart_ = nullptr;
+            e = cudaMalloc(&tstart_, sizeof(uint32_t) * (nkeys + 1));
+        }
+        if (e == cudaSuccess) e = cudaMemsetAsync(tcount, 0, nkeys * 4, st_);
+        if (e == cudaSuccess)
+            e = launch_tile_keys(row_, col_, reinterpret_cast<const float *>(val_), N_, urow_, keys, ids, rec, tcount,
+                                 st_);
+        if (e == cudaSuccess) e = exclusive_scan_u32(tcount, tstart_, nkeys, scr, st_);
+        if (e == cudaSuccess) e = radix_sort_pairs(keys, ids, keys2, ids2, n, key_bits, scr, st_);
+        if (e == cudaSuccess) e = launch_tile_gather(rec, ids, n, trec_, st_);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    }
+    release();
+    if (e != cudaSuccess) return fail("build_tiles", e);
+    tiles_ok_ = n > 0;
     return 0;
+}
+
+template <typename T>
+cudaError_t Embedding<T>::attr_call(const T *Yin, T *Yout, T *uY, T *gains, T *dC, const UpdateParams &p,
+                                    int shape) {
+    if constexpr (sizeof(T) == 4) {
+        if (shape == kAttrTilesShape && tiles_ok_)
+            return launch_attr_tiles_update(trec_, tstart_, acc_, Yin, Yout, uY, gains, dC, rep_, N_, D_, p, red_,
+                                            st_);
+    }
+    return launch_attr_update<T>(row_, col_, val_, Yin, Yout, uY, gains, dC, rep_, N_, D_, p, red_, st_,
+                                 shape >= kNumAttrShapes ? 10 : shape, yh_);
 }
 
 template <typename T>
@@ -296,12 +409,12 @@ int Embedding<T>::tune_fft(int M, int L) {
 
 template <typename T>
 void Embedding<T>::launch_shapes(int *out5) const {
-    int g = 0, u = 0;
-    attr_shape_info(attr_shape_, &g, &u);
+    int g = 4096, u = 4;
+    if (attr_shape_ != kAttrTilesShape) attr_shape_info(attr_shape_, &g, &u);
     out5[0] = attr_shape_;
     out5[1] = g;
     out5[2] = u;
-    out5[3] = 0;
+    out5[3] = (attr_shape_ == kAttrTilesShape && tiles_ok_) ? 2 : 0;
     out5[4] = fft_thr_;
 }
 
@@ -375,9 +488,8 @@ int Embedding<T>::gradient(double *dC_host, double *sum_Q) {
         int tr = tune_attr(false);
         if (tr) return tr;
     }
-    FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], nullptr, nullptr, nullptr, dC_, rep_, N_, D_, p,
-                                    red_, st_, attr_shape_, yh_));
-    launches_ += 2;
+    FITSNE_CK(attr_call(Y_[cur_], nullptr, nullptr, nullptr, dC_, p, attr_shape_));
+    launches_ += (attr_shape_ == kAttrTilesShape && tiles_ok_) ? 3 : 2;
     std::vector<T> tmp((size_t) N_ * D_);
     FITSNE_CK(cudaMemcpyAsync(tmp.data(), dC_, sizeof(T) * tmp.size(), cudaMemcpyDeviceToHost, st_));
     FITSNE_CK(cudaMemcpyAsync(h_pin_ + 2, red_.z, sizeof(double), cudaMemcpyDeviceToHost, st_));
@@ -450,6 +562,7 @@ int Embedding<T>::reorder() {
     std::swap(row_, row2_);
     std::swap(col_, col2_);
     std::swap(val_, val2_);
+    if (int rb = build_tiles()) return rb;
     // caller index of each internal point, and its inverse
     FITSNE_CK(launch_compose(perm_, order, rids2_, N_, st_));
     std::swap(perm_, rids2_);
@@ -482,9 +595,9 @@ int Embedding<T>::step(const UpdateParams &p, bool) {
         rc = tune_attr(true);
         if (rc) return rc;
     }
-    FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], uY_, gains_, nullptr, rep_, N_, D_, p,
-                                    red_, st_, attr_shape_, yh_));
-    launches_ += 2;  // centre + attraction
+    FITSNE_CK(attr_call(Y_[cur_], Y_[1 - cur_], uY_, gains_, nullptr, p, attr_shape_));
+    // centre + attraction (+ the separate update of the tiled form)
+    launches_ += (attr_shape_ == kAttrTilesShape && tiles_ok_) ? 3 : 2;
     if (timing_) {
         FITSNE_CK(cudaEventRecord(evs_[tb_][5], st_));
         tpend_ = true;
@@ -639,21 +752,23 @@ int Embedding<T>::tune_attr(bool measure) {
     // warps per SM on the expanded embedding, 8 x 4 on the compact one; FP64 (twice the
     // registers per value): 16 x 2 and 8 x 4 with 32 warps.
     static const int kCandidates32[] = {10, 2, 3, 0};
+    // FP32 with a symmetric P: the full-CSR default, the tiled form, the compact-phase shape
+    static const int kCandidatesTiles[] = {10, kAttrTilesShape, 2};
     static const int kCandidates64[] = {3, 2};
-    const int *kCandidates = sizeof(T) == 4 ? kCandidates32 : kCandidates64;
-    const int kNumCandidates = sizeof(T) == 4 ? 4 : 2;
+    const int *kCandidates = sizeof(T) == 4 ? (tiles_ok_ ? kCandidatesTiles : kCandidates32) : kCandidates64;
+    const int kNumCandidates = sizeof(T) == 4 ? (tiles_ok_ ? 3 : 4) : 2;
     static std::mutex mu;
     static std::map<std::vector<int>, int> chosen;
     int lgN = 0, lgK = 0;
     while ((1 << (lgN + 1)) <= N_) ++lgN;
     const size_t per = N_ ? nnz_ / (size_t) N_ : 0;
     while (((size_t) 1 << (lgK + 1)) <= per) ++lgK;
-    const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0, tune_phase_};
+    const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0, tune_phase_, tiles_ok_ ? 1 : 0};
     attr_phase_ = tune_phase_;
     const char *fixed = std::getenv("FITSNE_ATTR_SHAPE");  // a fixed shape index: no tuning, no cache
     if (fixed && *fixed) {
         const int sh = std::atoi(fixed);
-        attr_shape_ = (sh >= 0 && sh < kNumAttrShapes) ? sh : 0;
+        attr_shape_ = (sh >= 0 && sh <= kAttrTilesShape) ? sh : 0;
         return 0;
     }
     {
@@ -696,12 +811,9 @@ int Embedding<T>::tune_attr(bool measure) {
         float best_ms = 0.f;
         for (int ci = 0; ci < kNumCandidates; ++ci) {
             const int sh = kCandidates[ci];
-            FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr, rep_,
-                                            N_, D_, p, red_, st_, sh, yh_));
+            FITSNE_CK(attr_call(Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr, p, sh));
             FITSNE_CK(cudaEventRecord(a, st_));
-            for (int r = 0; r < 2; ++r)
-                FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr,
-                                                rep_, N_, D_, p, red_, st_, sh, yh_));
+            for (int r = 0; r < 2; ++r) FITSNE_CK(attr_call(Y_[cur_], Y_[1 - cur_], scr, scr + nd, nullptr, p, sh));
             FITSNE_CK(cudaEventRecord(b, st_));
             FITSNE_CK(cudaEventSynchronize(b));
             float ms = 0.f;
@@ -720,8 +832,8 @@ int Embedding<T>::tune_attr(bool measure) {
         FITSNE_CK(cudaStreamSynchronize(st_));
         FITSNE_CK(cudaFree(scr));
         if (timing_requested()) {
-            int g = 0, u = 0;
-            attr_shape_info(best, &g, &u);
+            int g = 4096, u = 4;  // the tiled form: 4,096-point blocks, 4 records per lane
+            if (best != kAttrTilesShape) attr_shape_info(best, &g, &u);
             std::fprintf(stderr, "[fitsne] attraction launch shape %d (N=%d, nnz=%zu%s, phase %d): %d rows per work "
                                  "item, %d edges per lane\n", best, N_, nnz_, reordered_ ? ", renumbered" : "",
                          tune_phase_, g, u);
@@ -815,8 +927,8 @@ int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_f
         else
             FITSNE_CK(conv1d_launch_dev<T>(grid_in_, grid_out_, L_cap_, cg, tw_dev_, work_a_, gp_.df, mode, st_));
         FITSNE_CK(launch_gather_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_out_, mode, rep_, red_, st_, yh_));
-        FITSNE_CK(launch_attr_update<T>(row_, col_, val_, Y_[c], Y_[1 - c], uY_, gains_, nullptr, rep_, N_, D_, p,
-                                        red_, st_, attr_shape_ < 0 ? (sizeof(T) == 4 ? 10 : 3) : attr_shape_, yh_));
+        FITSNE_CK(attr_call(Y_[c], Y_[1 - c], uY_, gains_, nullptr, p,
+                            attr_shape_ < 0 ? (sizeof(T) == 4 ? 10 : 3) : attr_shape_));
         c = 1 - c;
     }
     FITSNE_CK(cudaMemcpyAsync(h_gstat_, gstatus_, sizeof(int), cudaMemcpyDeviceToHost, st_));
@@ -850,7 +962,7 @@ int Embedding<T>::finish_chunk(int len) {
     nb_last_ = h_gstat_[1];
     if (len & 1) cur_ = 1 - cur_;
     mean_pending_ = true;
-    launches_ += (unsigned long long) len * (D_ == 2 ? 11 : 8);
+    launches_ += (unsigned long long) len * ((D_ == 2 ? 11 : 8) + ((attr_shape_ == kAttrTilesShape && tiles_ok_) ? 1 : 0));
     return 0;
 }
 
@@ -922,7 +1034,8 @@ std::vector<unsigned long long> Embedding<T>::chunk_key(const UpdateParams &p, i
     for (const void *q : {(const void *) row_, (const void *) col_, (const void *) val_, (const void *) Y_[0],
                           (const void *) Y_[1], (const void *) uY_, (const void *) gains_, (const void *) rep_,
                           (const void *) grid_in_, (const void *) grid_out_, (const void *) work_a_,
-                          (const void *) work_b_, (const void *) kspec_, (const void *) tw_dev_})
+                          (const void *) work_b_, (const void *) kspec_, (const void *) tw_dev_, (const void *) trec_,
+                          (const void *) tstart_, (const void *) acc_})
         put(&q, sizeof q);
     return key;
 }

@@ -189,6 +189,18 @@ class Embedding {
     // and the embedding's extent decide between the shapes
     int attr_shape_ = -1;
     int attr_phase_ = -1;  // tune_phase_ that attr_shape_ was chosen for
+    // The tiled attraction (FP32 form, symmetric P; shape kAttrTilesShape): records of the
+    // upper entries sorted by tile, the tiles' first records, the force accumulator.
+    bool sym_ok_ = false, tiles_ok_ = false;
+    uint32_t *urow_ = nullptr;
+    size_t unnz_ = 0;
+    uint2 *trec_ = nullptr;
+    uint32_t *tstart_ = nullptr;
+    float *acc_ = nullptr;
+    int check_symmetric();  // sets sym_ok_ (FP32 form, FITSNE_ATTR_SYM unset or 1), builds the tiles
+    int build_tiles();      // from the current CSR (after every renumbering)
+    // the attraction + update of the given shape (either form)
+    cudaError_t attr_call(const T *Yin, T *Yout, T *uY, T *gains, T *dC, const UpdateParams &p, int shape);
     int tune_phase_ = 1;   // phase of the current iteration (tune_phase)
     int tune_attr(bool measure);
     // autotuned threads per block of the 2-D FFT passes, per transform length (fft_thr_L_)

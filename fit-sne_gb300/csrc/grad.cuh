@@ -172,6 +172,29 @@ template <typename T>
 cudaError_t launch_attr_update(const uint32_t *row, const uint32_t *col, const T *val, const T *Yin, T *Yout,
                                T *uY, T *gains, T *dC, const T *rep, int N, int D, const UpdateParams &p,
                                RedScratch r, cudaStream_t st, int shape = 0, const float *yh = nullptr);
+// ---- tiled attraction over the half-stored symmetric P (FP32 form; k_attr_tiles in grad.cu) ----
+// Shape index of the tiled form, after the full-CSR shapes (FITSNE_ATTR_SHAPE numbering).
+constexpr int kAttrTilesShape = kNumAttrShapes;
+// h[0..1] (device): hash sums of the entries and of their transposes; equal iff P is
+// symmetric (entries and values), up to a 2^-64 chance.
+cudaError_t launch_sym_hash(const uint32_t *row, const uint32_t *col, const float *val, int N,
+                            unsigned long long *h, cudaStream_t st);
+// ulen[i]: entries of row i with col > i.
+cudaError_t launch_upper_count(const uint32_t *row, const uint32_t *col, int N, uint32_t *ulen, cudaStream_t st);
+// Blocks of 4,096 points: tile_blocks(N) of them, tile keys A * nblk + B (A <= B).
+int tile_blocks(int N);
+size_t tile_smem_bytes(int D);
+// Per upper entry of the CSR (urow: the exclusive scan of the upper counts): key, index and
+// record; tcount (nblk^2, zero on entry) receives the tile sizes.
+cudaError_t launch_tile_keys(const uint32_t *row, const uint32_t *col, const float *val, int N, const uint32_t *urow,
+                             uint32_t *keys, uint32_t *ids, uint2 *rec, uint32_t *tcount, cudaStream_t st);
+cudaError_t launch_tile_gather(const uint2 *rec, const uint32_t *ids, size_t n, uint2 *trec, cudaStream_t st);
+// trec: records sorted by tile key (row order within a tile); tstart[nblk^2 + 1]: the tiles'
+// first records.  The attraction into acc (N x D floats, zero on entry), then the update of
+// launch_attr_update (dC in mode 0), which clears acc again.
+cudaError_t launch_attr_tiles_update(const uint2 *trec, const uint32_t *tstart, float *acc, const float *Yin,
+                                     float *Yout, float *uY, float *gains, float *dC, const float *rep, int N, int D,
+                                     const UpdateParams &p, RedScratch r, cudaStream_t st);
 template <typename T>
 cudaError_t launch_kl(const uint32_t *row, const uint32_t *col, const T *val, const T *Y, int N, int D, double exag,
                       double df, RedScratch r, cudaStream_t st);

@@ -3,6 +3,8 @@
 Tolerances: the FP32 form must stay within relative L2 1e-4 of the reference's FP64
 gradient on identical Y and P (the stated target) and Z within 1e-5; the FP64 form must
 agree to rounding (1e-9)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -104,7 +106,9 @@ def test_fp32_box_index_agrees_with_fp64_on_a_box_edge(gpu_lib, golden):
     assert rel_l2(g32, g64) < 1e-5
 
 
-N_SHAPES = 11  # attraction launch shapes (kNumAttrShapes)
+# attraction launch shapes: 11 over the full CSR (kNumAttrShapes), then the tiled form over the
+# half-stored symmetric P (kAttrTilesShape = 11; FP32 form, the FP64 form takes shape 10 for it)
+N_SHAPES = 12
 
 
 @pytest.mark.parametrize("shape", range(N_SHAPES))
@@ -164,3 +168,73 @@ def test_every_fft_block_size_gives_the_reference_gradient(gpu_lib, golden, monk
     assert rel_l2(dC, golden["g2_df1_dC"]) < TOL[bits][0]
     assert abs(z - float(golden["g2_df1_Z"])) < TOL[bits][1] * float(golden["g2_df1_Z"])
     assert rel_l2(dC5, golden["g2_nt5_dC"]) < TOL[bits][0]
+
+
+def test_tiled_attraction_runs_for_a_symmetric_P(gpu_lib, golden, monkeypatch):
+    """With a symmetric P the FP32 form's tiled shape runs two kernels (attraction into the
+    accumulator, then the update): one launch per iteration more than the full-CSR shapes,
+    and the same steps within the FP32 tolerance."""
+    row, col, val = _P(golden)
+    launches, ys = {}, {}
+    for shape in (10, 11):
+        monkeypatch.setenv("FITSNE_ATTR_SHAPE", str(shape))
+        s = gpu_lib.Session(row, col, val, golden["Y2"], precision=32)
+        try:
+            s.set_graphs(False)
+            s.run(300, 310, learning_rate=200.0)
+            launches[shape] = s.stage_times()[9]
+            ys[shape] = s.get_y()
+            assert s.launch_shapes()["attr_form"] == (2 if shape == 11 else 0)
+        finally:
+            s.close()
+    assert launches[11] == launches[10] + 10, launches
+    assert rel_l2(ys[11], ys[10]) < 1e-4
+
+
+def test_tiled_attraction_falls_back_on_an_asymmetric_P(gpu_lib, golden, monkeypatch):
+    """The calibrated kNN matrix before symmetrisation is not symmetric: the tiled shape must
+    detect it and take the full CSR (the reference's attraction works for any P)."""
+    monkeypatch.setenv("FITSNE_ATTR_SHAPE", "11")
+    row, col, val = golden["knn_row"], golden["knn_col"], golden["knn_val"] / golden["knn_val"].sum()
+    d32, _ = gpu_lib.fft_gradient(row, col, val, golden["Y2"], 3, 1.0, 50, 1.0)
+    gpu_lib.set_precision(64)
+    try:
+        d64, _ = gpu_lib.fft_gradient(row, col, val, golden["Y2"], 3, 1.0, 50, 1.0)
+    finally:
+        gpu_lib.set_precision(32)
+    assert rel_l2(d32, d64) < 1e-4
+
+
+def test_tiled_attraction_across_many_tiles_and_renumberings(gpu_lib, monkeypatch):
+    """The tiled attraction on 30,000 points: 8 blocks of 4,096, so up to 36 tiles, and a last
+    block of 1,328 points.  A session runs 310 iterations with it, through the locality
+    renumberings at 50, 150 and 300 (the tiles are rebuilt after each); its gradient at the end
+    matches the restated reference gradient (FP64) on the same Y and P, and the full-CSR
+    shape's."""
+    import oracle
+    oracle.build_restated()
+    orc = oracle.Restated()
+    rng = np.random.default_rng(30)
+    c = rng.standard_normal((12, 20)) * 4.0
+    X = c[rng.integers(0, 12, 30000)] + rng.standard_normal((30000, 20))
+    X = X - np.cumsum(X, axis=0)[-1] / len(X)
+    X /= np.abs(X).max()
+    row, col, val = gpu_lib.gaussian_perplexity(X, 30.0, 90)
+    row, col, val = gpu_lib.symmetrize(row, col, val, len(X))
+    val = val / np.cumsum(val)[-1]
+    Y0 = rng.standard_normal((len(X), 2)) * 1e-4
+    monkeypatch.setenv("FITSNE_ATTR_SHAPE", "11")
+    s = gpu_lib.Session(row, col, val, Y0, precision=32)
+    try:
+        s.run(0, 310, learning_rate=len(X) / 12.0)
+        assert s.launch_shapes()["attr_form"] == 2
+        Y = s.get_y()
+        d11, z11 = s.gradient()
+    finally:
+        s.close()
+    dref, zref = orc.fft_gradient(row, col, val, Y, 3, 1.0, 50, os.cpu_count() or 4, 1.0)
+    assert rel_l2(d11, dref) < 1e-4
+    assert abs(z11 - zref) < 1e-5 * zref
+    monkeypatch.setenv("FITSNE_ATTR_SHAPE", "10")
+    d10, _ = gpu_lib.fft_gradient(row, col, val, Y, 3, 1.0, 50, 1.0)
+    assert rel_l2(d11, d10) < 1e-4

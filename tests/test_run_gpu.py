@@ -218,6 +218,37 @@ def test_batched_jobs_match_single_runs(gpu_lib, monkeypatch, mode):
     assert abs(costs[0][499] - g["df1"][499]) <= 1e-2 * g["df1"][499]
 
 
+def test_sixteen_batched_jobs_of_uneven_size(gpu_lib, orc):
+    """16 jobs, N log-uniform in [1,500, 12,000], 5 - 15 clusters each, perplexity 10 / 30 / 50
+    cycled (K = 3 perplexity), advanced together by the all-jobs pipeline: each job's final KL
+    within 1.5 % of the mean of two single runs of the same job, and the smallest job's within
+    1 % of the restated reference loop run on the reference's P from the same start."""
+    rng = np.random.default_rng(16)
+    Xs, perps = [], []
+    for j in range(16):
+        N = int(round(np.exp(rng.uniform(np.log(1500), np.log(12000)))))
+        k = int(rng.integers(5, 16))
+        c = rng.standard_normal((k, 20)) * 5.0
+        Xs.append(c[rng.integers(0, k, N)] + rng.standard_normal((N, 20)))
+        perps.append((10.0, 30.0, 50.0)[j % 3])
+    Y0s = [rng.standard_normal((len(X), 2)) * 1e-4 for X in Xs]
+    lrs = [max(200.0, len(X) / 12.0) for X in Xs]
+    Ys, costs, st = gpu_lib.batch_run(Xs, perps, learning_rates=lrs, Y0s=Y0s, max_iter=500)
+    assert st["graph_launches"] >= 9
+    for j, X in enumerate(Xs):
+        ref = np.mean([gpu_lib.run(X, Y0=Y0s[j], perplexity=perps[j], learning_rate=lrs[j], max_iter=500,
+                                   knn_algo=2)[1][499] for _ in range(2)])
+        assert np.isfinite(Ys[j]).all()
+        assert abs(costs[j][499] - ref) <= 1.5e-2 * ref, (j, len(X), costs[j][499], ref)
+    j = int(np.argmin([len(X) for X in Xs]))
+    X = Xs[j] - np.cumsum(Xs[j], axis=0)[-1] / len(Xs[j])
+    X /= np.abs(X).max()
+    r, c, v = gpu_lib.gaussian_perplexity(X, perps[j], int(3 * perps[j]))
+    r, c, v = gpu_lib.symmetrize(r, c, v, len(X))
+    _, cref = orc.run_from_P(r, c, v / np.cumsum(v)[-1], Y0s[j], max_iter=500, learning_rate=lrs[j], nthreads=4)
+    assert abs(costs[j][499] - cref[499]) <= 1e-2 * cref[499], (costs[j][499], cref[499])
+
+
 def test_batched_one_dimensional_jobs(gpu_lib):
     """1-D batches (outside the all-jobs pipeline: one graph per job) end where the jobs' own
     runs end (final KL within 2 %: 800-point FP32 runs)."""
