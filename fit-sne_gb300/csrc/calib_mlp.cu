@@ -22,7 +22,7 @@ constexpr int H = kMlpHidden;
 constexpr int kSPB = 8;          // samples per block in the gradient kernel
 constexpr int kBatch = 512;      // minibatch (FITSNE_MLP_BATCH overrides)
 constexpr int kGraphSteps = 25;  // optimiser steps per captured graph
-constexpr float kLr = 2e-3f;     // Adam step size
+constexpr float kLr = 3e-3f;     // Adam step size (FITSNE_MLP_LR overrides)
 constexpr int kH2 = H + 1;       // padded row stride of W2 in shared memory
 
 struct Offs {
@@ -75,13 +75,15 @@ __device__ __forceinline__ unsigned mix32(unsigned a, unsigned b) {
 
 // ---- forward + backward of one minibatch ----------------------------------------------------
 // 64 threads (one per hidden unit) per block, kSPB samples per block, gradients accumulated
-// per block in shared memory and added to `grad` (FP32 atomics).  Standardised target
+// per block in shared memory and stored as the block's partial gradient, gpart[block][n]
+// (no atomics: the partials are summed in block order by k_adam / k_grad_sum, so training is
+// repeatable).  Standardised target
 // (target - mu) / sd; loss = mean squared error over the batch.  With step == nullptr the
 // batch is rows 0 .. batch-1 in order, else rows drawn by a hash of (step, position).
 __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params, int K, const float *__restrict__ x,
                                                  const float *__restrict__ target, int nrows, int batch, float mu,
                                                  float inv_sd, const unsigned *__restrict__ step,
-                                                 float *__restrict__ grad, double *__restrict__ loss) {
+                                                 float *__restrict__ gpart, double *__restrict__ loss) {
     extern __shared__ float sm[];
     const int KP = odd_stride(K);
     float *W1 = sm;
@@ -95,15 +97,18 @@ __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params
     const unsigned full = 0xffffffffu;
     const int u = threadIdx.x;
     const Offs o = offs(K);
-    for (int e = u; e < H * K; e += H) {
-        const int r = e / K, c = e % K;
-        W1[r * KP + c] = params[o.w1 + e];
-        gW1[r * KP + c] = 0.f;
-    }
-    for (int e = u; e < H * H; e += H) {
-        const int r = e / H, c = e % H;
-        W2[r * kH2 + c] = params[o.w2 + e];
-        gW2[r * kH2 + c] = 0.f;
+    // weights into shared memory, row by row with the rows unrolled, so that many independent
+    // loads are in flight (this load is the latency chain of a training step)
+#pragma unroll 8
+    for (int r = 0; r < H; ++r)
+        for (int c = u; c < K; c += H) {
+            W1[r * KP + c] = params[o.w1 + r * K + c];
+            gW1[r * KP + c] = 0.f;
+        }
+#pragma unroll 8
+    for (int r = 0; r < H; ++r) {
+        W2[r * kH2 + u] = params[o.w2 + r * H + u];
+        gW2[r * kH2 + u] = 0.f;
     }
     const float b1 = params[o.b1 + u], b2 = params[o.b2 + u], w3 = params[o.w3 + u], b3 = params[o.b3];
     float gb1 = 0.f, gb2 = 0.f, gw3 = 0.f, gb3 = 0.f;
@@ -145,14 +150,27 @@ __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params
         for (int j = 0; j < K; ++j) gW1[u * KP + j] = fmaf(d1, xs[j], gW1[u * KP + j]);
         __syncthreads();
     }
-    for (int e = u; e < H * K; e += H) atomicAdd(&grad[o.w1 + e], gW1[(e / K) * KP + e % K]);
-    for (int e = u; e < H * H; e += H) atomicAdd(&grad[o.w2 + e], gW2[(e / H) * kH2 + e % H]);
-    atomicAdd(&grad[o.b1 + u], gb1);
-    atomicAdd(&grad[o.b2 + u], gb2);
-    atomicAdd(&grad[o.w3 + u], gw3);
+    float *g = gpart + (size_t) blockIdx.x * o.n;
+#pragma unroll 8
+    for (int r = 0; r < H; ++r)
+        for (int c = u; c < K; c += H) g[o.w1 + r * K + c] = gW1[r * KP + c];
+#pragma unroll 8
+    for (int r = 0; r < H; ++r) g[o.w2 + r * H + u] = gW2[r * kH2 + u];
+    g[o.b1 + u] = gb1;
+    g[o.b2 + u] = gb2;
+    g[o.w3 + u] = gw3;
     if (u == 0) {
-        atomicAdd(&grad[o.b3], gb3);
+        g[o.b3] = gb3;
         atomicAdd(loss, lsum);
+    }
+}
+
+// grad[i] = sum over the blocks' partials, in block order
+__global__ void k_grad_sum(const float *__restrict__ gpart, int nblocks, int n, float *__restrict__ grad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float g = 0.f;
+        for (int b = 0; b < nblocks; ++b) g += gpart[(size_t) b * n + i];
+        grad[i] = g;
     }
 }
 
@@ -161,27 +179,36 @@ size_t grad_smem(int K) {
     return sizeof(float) * (2 * (size_t) H * KP + 2 * (size_t) H * kH2 + KP + 2 * H + 2);
 }
 
-// ---- Adam (one block): update, zero the gradient, record the loss, advance the step --------
-__global__ void __launch_bounds__(1024) k_adam(float *__restrict__ params, float *__restrict__ grad,
-                                               float *__restrict__ m, float *__restrict__ v, int n,
-                                               unsigned *__restrict__ step, double *__restrict__ loss_acc,
-                                               float *__restrict__ loss_hist, int batch) {
+// ---- Adam: sum of the partial gradients (block order), update; the last block out records
+// the loss and advances the step (every block reads the step before any block advances it:
+// the counter is only touched after the reads) ---------------------------------------------
+__global__ void __launch_bounds__(256) k_adam(float *__restrict__ params, const float *__restrict__ gpart,
+                                              int nblocks, float *__restrict__ m, float *__restrict__ v, int n,
+                                              unsigned *__restrict__ step, unsigned *__restrict__ done,
+                                              double *__restrict__ loss_acc, float *__restrict__ loss_hist,
+                                              int batch, float lr) {
     const unsigned t = *step + 1u;
     const float c1 = 1.f - powf(0.9f, (float) t), c2 = 1.f - powf(0.999f, (float) t);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float g = grad[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float g = 0.f;
+#pragma unroll 8
+        for (int b = 0; b < nblocks; ++b) g += gpart[(size_t) b * n + i];
         const float mi = 0.9f * m[i] + 0.1f * g;
         const float vi = 0.999f * v[i] + 0.001f * g * g;
         m[i] = mi;
         v[i] = vi;
-        params[i] -= kLr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
-        grad[i] = 0.f;
+        params[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + 1e-8f);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        loss_hist[t - 1] = (float) (*loss_acc / batch);
-        *loss_acc = 0.0;
-        *step = t;
+        __threadfence();
+        const unsigned prev = atomicAdd(done, 1u);
+        if (prev == gridDim.x - 1) {
+            loss_hist[t - 1] = (float) (*loss_acc / batch);
+            *loss_acc = 0.0;
+            *step = t;
+            *done = 0u;
+        }
     }
 }
 
@@ -431,18 +458,18 @@ int calibrate_rows_learned(const double *dist, int stride, int offset, double *P
     float *x = nullptr, *scale = nullptr, *target = nullptr, *params = nullptr, *grad = nullptr, *m = nullptr,
           *v = nullptr, *hist = nullptr;
     double *beta = nullptr, *loss = nullptr, *beta_hat = nullptr;
-    unsigned *step = nullptr;
+    unsigned *step = nullptr, *done = nullptr;
     int *iters = nullptr, *fb = nullptr;
     MCK(b.get(&x, (size_t) nrows * K));
     MCK(b.get(&scale, (size_t) nrows));
     MCK(b.get(&target, (size_t) nh));
     MCK(b.get(&beta, (size_t) nh));
     MCK(b.get(&params, (size_t) o.n));
-    MCK(b.get(&grad, (size_t) o.n));
     MCK(b.get(&m, (size_t) o.n));
     MCK(b.get(&v, (size_t) o.n));
     MCK(b.get(&loss, 1));
     MCK(b.get(&step, 1));
+    MCK(b.get(&done, 1));
     MCK(b.get(&beta_hat, (size_t) (nrows - nh)));
     MCK(b.get(&iters, (size_t) (nrows - nh)));
     MCK(b.get(&fb, (size_t) (nrows - nh)));
@@ -473,29 +500,35 @@ int calibrate_rows_learned(const double *dist, int stride, int offset, double *P
     // 3. training: Adam on random minibatches, kGraphSteps steps per captured graph
     std::vector<float> p0 = init_params(K);
     MCK(cudaMemcpyAsync(params, p0.data(), sizeof(float) * o.n, cudaMemcpyHostToDevice, st));
-    MCK(cudaMemsetAsync(grad, 0, sizeof(float) * o.n, st));
     MCK(cudaMemsetAsync(m, 0, sizeof(float) * o.n, st));
     MCK(cudaMemsetAsync(v, 0, sizeof(float) * o.n, st));
     MCK(cudaMemsetAsync(loss, 0, sizeof(double), st));
     MCK(cudaMemsetAsync(step, 0, sizeof(unsigned), st));
-    // 300 steps of 512 rows (FITSNE_MLP_STEPS / FITSNE_MLP_BATCH override): the search only
-    // needs a seed within a few per cent of beta; its FP32 Newton steps correct the rest at
-    // little cost, and the FP64 evaluations it needs do not depend on the seed's accuracy
-    int batch = kBatch, want = 300;
+    MCK(cudaMemsetAsync(done, 0, sizeof(unsigned), st));
+    // 600 steps of 512 rows at step size 3e-3 (FITSNE_MLP_STEPS / FITSNE_MLP_BATCH /
+    // FITSNE_MLP_LR override): the search only needs a seed within a few per cent of beta.
+    // Measured (N = 1M and 60,000): the entropy evaluations per predicted row (4.0 - 4.6) and
+    // the time of the search hardly depend on the training beyond that; its FP32 Newton
+    // steps correct the rest at little cost.
+    int batch = kBatch, want = 600;
     if (const char *eb = std::getenv("FITSNE_MLP_BATCH")) batch = std::max(kSPB, std::min(8192, std::atoi(eb)));
     if (const char *es = std::getenv("FITSNE_MLP_STEPS")) want = std::max(kGraphSteps, std::min(20000, std::atoi(es)));
     const int nsteps = want / kGraphSteps * kGraphSteps;
+    float lr = kLr;
+    if (const char *el = std::getenv("FITSNE_MLP_LR")) lr = std::max(1e-5f, std::min(0.1f, (float) std::atof(el)));
     MCK(b.get(&hist, (size_t) nsteps));
     const size_t gsm = grad_smem(K);
     MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) gsm));
     const int gblocks = (batch + kSPB - 1) / kSPB;
+    MCK(b.get(&grad, (size_t) gblocks * o.n));  // the blocks' partial gradients
+    const int ablocks = (o.n + 255) / 256;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     MCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < kGraphSteps; ++k) {
         k_mlp_grad<<<gblocks, H, gsm, st>>>(params, K, x, target, nh, batch, (float) mu, (float) (1.0 / sd), step,
                                             grad, loss);
-        k_adam<<<1, 1024, 0, st>>>(params, grad, m, v, o.n, step, loss, hist, batch);
+        k_adam<<<ablocks, 256, 0, st>>>(params, grad, gblocks, m, v, o.n, step, done, loss, hist, batch, lr);
     }
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
     if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
@@ -569,8 +602,11 @@ int mlp_loss_grad_host(const float *params, int K, const double *dist, const dou
     Bufs b;
     float *dp = nullptr, *dg = nullptr, *x = nullptr, *scale = nullptr, *target = nullptr;
     double *dd = nullptr, *db = nullptr, *dl = nullptr;
+    const int gblocks = (nrows + kSPB - 1) / kSPB;
+    float *gp = nullptr;
     MCK(b.get(&dp, (size_t) o.n));
     MCK(b.get(&dg, (size_t) o.n));
+    MCK(b.get(&gp, (size_t) gblocks * o.n));
     MCK(b.get(&dd, (size_t) nrows * K));
     MCK(b.get(&db, (size_t) nrows));
     MCK(b.get(&x, (size_t) nrows * K));
@@ -580,13 +616,12 @@ int mlp_loss_grad_host(const float *params, int K, const double *dist, const dou
     MCK(cudaMemcpy(dp, params, sizeof(float) * o.n, cudaMemcpyHostToDevice));
     MCK(cudaMemcpy(dd, dist, sizeof(double) * (size_t) nrows * K, cudaMemcpyHostToDevice));
     MCK(cudaMemcpy(db, beta, sizeof(double) * nrows, cudaMemcpyHostToDevice));
-    MCK(cudaMemset(dg, 0, sizeof(float) * o.n));
     MCK(cudaMemset(dl, 0, sizeof(double)));
     k_features<<<256, 256>>>(dd, K, 0, nrows, K, db, x, scale, target);
     const size_t gsm = grad_smem(K);
     MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) gsm));
-    k_mlp_grad<<<(nrows + kSPB - 1) / kSPB, H, gsm>>>(dp, K, x, target, nrows, nrows, (float) mu, (float) (1.0 / sd),
-                                                      nullptr, dg, dl);
+    k_mlp_grad<<<gblocks, H, gsm>>>(dp, K, x, target, nrows, nrows, (float) mu, (float) (1.0 / sd), nullptr, gp, dl);
+    k_grad_sum<<<(o.n + 255) / 256, 256>>>(gp, gblocks, o.n, dg);
     MCK(cudaGetLastError());
     MCK(cudaDeviceSynchronize());
     MCK(cudaMemcpy(grad, dg, sizeof(float) * o.n, cudaMemcpyDeviceToHost));
