@@ -265,6 +265,23 @@ int Embedding<T>::build_tiles() {
         if (e == cudaSuccess) e = radix_sort_pairs(keys, ids, keys2, ids2, n, key_bits, scr, st_);
         if (e == cudaSuccess) e = launch_tile_gather(rec, ids, n, trec_, st_);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+        if (e == cudaSuccess && timing_requested()) {
+            // how the edges spread over the tiles: the tiled form pays per tile (a block load
+            // and an accumulator flush), so it gains where the tiles are dense
+            std::vector<uint32_t> tc(nkeys);
+            e = cudaMemcpy(tc.data(), tcount, nkeys * 4, cudaMemcpyDeviceToHost);
+            size_t ne = 0, e4 = 0, e16 = 0, e64 = 0;
+            for (uint32_t c : tc) {
+                ne += c > 0;
+                e4 += c >= 4096 ? c : 0;
+                e16 += c >= 16384 ? c : 0;
+                e64 += c >= 65536 ? c : 0;
+            }
+            std::fprintf(stderr,
+                         "[fitsne] tiles: N=%d, %d blocks, %zu of %zu tiles hold edges, %zu upper edges; share of edges "
+                         "in tiles of >= 4096 / 16384 / 65536 edges: %.3f / %.3f / %.3f\n",
+                         N_, nblk, ne, nkeys, n, (double) e4 / n, (double) e16 / n, (double) e64 / n);
+        }
     }
     release();
     if (e != cudaSuccess) return fail("build_tiles", e);
