@@ -1025,7 +1025,7 @@ __global__ void __launch_bounds__(kBlock)
 
 constexpr int kTileShift = 12;
 constexpr int kTileRows = 1 << kTileShift;
-constexpr int kTileThreads = 512;
+constexpr int kTileThreads = 1024;
 
 // per upper entry (a warp per row, ballot compaction, row order): its tile key A * nblk + B,
 // its index, and its record; tile sizes counted into tcount
