@@ -90,8 +90,9 @@ __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params
     float *W2 = W1 + H * KP;
     float *gW1 = W2 + H * kH2;
     float *gW2 = gW1 + H * KP;
-    float *xs = gW2 + H * kH2;
-    float *h1 = xs + KP;
+    float *xall = gW2 + H * kH2;  // the block's kSPB samples (prefetched), then their targets
+    float *tall = xall + kSPB * KP;
+    float *h1 = tall + kSPB;
     float *dh2 = h1 + H;
     float *red = dh2 + H;
     const unsigned full = 0xffffffffu;
@@ -114,13 +115,21 @@ __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params
     float gb1 = 0.f, gb2 = 0.f, gw3 = 0.f, gb3 = 0.f;
     double lsum = 0.0;
     const unsigned stp = step ? *step : 0u;
+    // all of the block's samples and targets in one round of loads (not one dependent global
+    // load per sample between the barriers)
+#pragma unroll
+    for (int q = 0; q < kSPB; ++q) {
+        const int pos = blockIdx.x * kSPB + q;
+        if (pos >= batch) break;
+        const int row = step ? (int) (mix32(stp, (unsigned) pos) % (unsigned) nrows) : pos;
+        for (int j = u; j < K; j += H) xall[q * KP + j] = x[(size_t) row * K + j];
+        if (u == 0) tall[q] = target[row];
+    }
     __syncthreads();
     for (int q = 0; q < kSPB; ++q) {
         const int pos = blockIdx.x * kSPB + q;
         if (pos >= batch) break;  // uniform over the block
-        const int row = step ? (int) (mix32(stp, (unsigned) pos) % (unsigned) nrows) : pos;
-        for (int j = u; j < K; j += H) xs[j] = x[(size_t) row * K + j];
-        __syncthreads();
+        const float *xs = xall + q * KP;
         float a1 = b1;
         for (int j = 0; j < K; ++j) a1 = fmaf(W1[u * KP + j], xs[j], a1);
         h1[u] = a1 > 0.f ? a1 : 0.f;
@@ -133,7 +142,7 @@ __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params
         if ((u & 31) == 0) red[u >> 5] = p;
         __syncthreads();
         const float out = red[0] + red[1] + b3;
-        const float err = out - (target[row] - mu) * inv_sd;
+        const float err = out - (tall[q] - mu) * inv_sd;
         if (u == 0) lsum += (double) err * err;
         const float dout = 2.f * err / (float) batch;
         gw3 = fmaf(dout, r2, gw3);
@@ -176,7 +185,7 @@ __global__ void k_grad_sum(const float *__restrict__ gpart, int nblocks, int n, 
 
 size_t grad_smem(int K) {
     const int KP = odd_stride(K);
-    return sizeof(float) * (2 * (size_t) H * KP + 2 * (size_t) H * kH2 + KP + 2 * H + 2);
+    return sizeof(float) * (2 * (size_t) H * KP + 2 * (size_t) H * kH2 + (size_t) kSPB * (KP + 1) + 2 * H + 2);
 }
 
 // ---- Adam: sum of the partial gradients (block order), update; the last block out records
