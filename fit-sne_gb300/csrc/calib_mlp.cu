@@ -19,7 +19,7 @@ namespace fitsne {
 namespace {
 
 constexpr int H = kMlpHidden;
-constexpr int kSPB = 8;          // samples per block in the gradient kernel
+constexpr int kSPB = 16;         // samples per block in the gradient kernel (all carried at once)
 constexpr int kBatch = 512;      // minibatch (FITSNE_MLP_BATCH overrides)
 constexpr int kGraphSteps = 25;  // optimiser steps per captured graph
 constexpr float kLr = 3e-3f;     // Adam step size (FITSNE_MLP_LR overrides)
@@ -74,97 +74,132 @@ __device__ __forceinline__ unsigned mix32(unsigned a, unsigned b) {
 }
 
 // ---- forward + backward of one minibatch ----------------------------------------------------
-// 64 threads (one per hidden unit) per block, kSPB samples per block, gradients accumulated
-// per block in shared memory and stored as the block's partial gradient, gpart[block][n]
-// (no atomics: the partials are summed in block order by k_adam / k_grad_sum, so training is
-// repeatable).  Standardised target
-// (target - mu) / sd; loss = mean squared error over the batch.  With step == nullptr the
-// batch is rows 0 .. batch-1 in order, else rows drawn by a hash of (step, position).
+// 64 threads (one per hidden unit) per block and kSPB samples per block, all carried at once
+// by every thread (kSPB independent accumulation chains; every weight read once for the
+// block's samples).  Each weight's gradient over the block's samples is complete after one
+// pass, so it goes straight to the block's partial gradient gpart[block][n] (no atomics: the
+// partials are summed in block order by k_adam / k_grad_sum, so training is repeatable).
+// In the partials the two weight matrices are stored transposed (part_index), so that the
+// 64 threads of a block write consecutive words.  Standardised target (target - mu) / sd;
+// loss = mean squared error over the batch.  With step == nullptr the batch is rows
+// 0 .. batch-1 in order, else rows drawn by a hash of (step, position).
+__host__ __device__ inline int part_index(int i, const Offs &o, int K) {
+    if (i < o.b1) return o.w1 + (i % K) * H + i / K;
+    if (i >= o.w2 && i < o.b2) return o.w2 + ((i - o.w2) % H) * H + (i - o.w2) / H;
+    return i;
+}
+
 __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params, int K, const float *__restrict__ x,
                                                  const float *__restrict__ target, int nrows, int batch, float mu,
                                                  float inv_sd, const unsigned *__restrict__ step,
                                                  float *__restrict__ gpart, double *__restrict__ loss) {
+    constexpr int S = kSPB;
     extern __shared__ float sm[];
     const int KP = odd_stride(K);
-    float *W1 = sm;
-    float *W2 = W1 + H * KP;
-    float *gW1 = W2 + H * kH2;
-    float *gW2 = gW1 + H * KP;
-    float *xall = gW2 + H * kH2;  // the block's kSPB samples (prefetched), then their targets
-    float *tall = xall + kSPB * KP;
-    float *h1 = tall + kSPB;
-    float *dh2 = h1 + H;
-    float *red = dh2 + H;
+    float *W1 = sm;             // [H][KP]
+    float *W2 = W1 + H * KP;    // [H][kH2]
+    float *xt = W2 + H * kH2;   // samples, transposed: [K][S]
+    float *tt = xt + K * S;     // targets [S]
+    float *h1t = tt + S;        // [H][S]
+    float *dh2t = h1t + H * S;  // [H][S]
+    float *red = dh2t + H * S;  // [S][2 warps]
     const unsigned full = 0xffffffffu;
     const int u = threadIdx.x;
     const Offs o = offs(K);
-    // weights into shared memory, row by row with the rows unrolled, so that many independent
-    // loads are in flight (this load is the latency chain of a training step)
 #pragma unroll 8
     for (int r = 0; r < H; ++r)
-        for (int c = u; c < K; c += H) {
-            W1[r * KP + c] = params[o.w1 + r * K + c];
-            gW1[r * KP + c] = 0.f;
-        }
+        for (int c = u; c < K; c += H) W1[r * KP + c] = params[o.w1 + r * K + c];
 #pragma unroll 8
-    for (int r = 0; r < H; ++r) {
-        W2[r * kH2 + u] = params[o.w2 + r * H + u];
-        gW2[r * kH2 + u] = 0.f;
-    }
+    for (int r = 0; r < H; ++r) W2[r * kH2 + u] = params[o.w2 + r * H + u];
     const float b1 = params[o.b1 + u], b2 = params[o.b2 + u], w3 = params[o.w3 + u], b3 = params[o.b3];
-    float gb1 = 0.f, gb2 = 0.f, gw3 = 0.f, gb3 = 0.f;
-    double lsum = 0.0;
     const unsigned stp = step ? *step : 0u;
-    // all of the block's samples and targets in one round of loads (not one dependent global
-    // load per sample between the barriers)
+    // the block's samples and targets in one round of loads; samples past the batch are zero
 #pragma unroll
-    for (int q = 0; q < kSPB; ++q) {
-        const int pos = blockIdx.x * kSPB + q;
-        if (pos >= batch) break;
-        const int row = step ? (int) (mix32(stp, (unsigned) pos) % (unsigned) nrows) : pos;
-        for (int j = u; j < K; j += H) xall[q * KP + j] = x[(size_t) row * K + j];
-        if (u == 0) tall[q] = target[row];
+    for (int q = 0; q < S; ++q) {
+        const int pos = blockIdx.x * S + q;
+        const bool valid = pos < batch;
+        const int row = !valid ? 0 : (step ? (int) (mix32(stp, (unsigned) pos) % (unsigned) nrows) : pos);
+        for (int j = u; j < K; j += H) xt[j * S + q] = valid ? x[(size_t) row * K + j] : 0.f;
+        if (u == 0) tt[q] = valid ? target[row] : 0.f;
     }
     __syncthreads();
-    for (int q = 0; q < kSPB; ++q) {
-        const int pos = blockIdx.x * kSPB + q;
-        if (pos >= batch) break;  // uniform over the block
-        const float *xs = xall + q * KP;
-        float a1 = b1;
-        for (int j = 0; j < K; ++j) a1 = fmaf(W1[u * KP + j], xs[j], a1);
-        h1[u] = a1 > 0.f ? a1 : 0.f;
-        __syncthreads();
-        float a2 = b2;
-        for (int k = 0; k < H; ++k) a2 = fmaf(W2[u * kH2 + k], h1[k], a2);
-        const float r2 = a2 > 0.f ? a2 : 0.f;
-        float p = w3 * r2;
-        for (int off = 16; off; off >>= 1) p += __shfl_xor_sync(full, p, off);
-        if ((u & 31) == 0) red[u >> 5] = p;
-        __syncthreads();
-        const float out = red[0] + red[1] + b3;
-        const float err = out - (tall[q] - mu) * inv_sd;
-        if (u == 0) lsum += (double) err * err;
+    // forward, layer 1
+    float a1[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) a1[q] = b1;
+    for (int j = 0; j < K; ++j) {
+        const float w = W1[u * KP + j];
+#pragma unroll
+        for (int q = 0; q < S; ++q) a1[q] = fmaf(w, xt[j * S + q], a1[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < S; ++q) h1t[u * S + q] = a1[q] > 0.f ? a1[q] : 0.f;
+    __syncthreads();
+    // layer 2
+    float a2[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) a2[q] = b2;
+    for (int k = 0; k < H; ++k) {
+        const float w = W2[u * kH2 + k];
+#pragma unroll
+        for (int q = 0; q < S; ++q) a2[q] = fmaf(w, h1t[k * S + q], a2[q]);
+    }
+    // output of each sample: w3 . relu(a2) over the 64 units (two warps)
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+        float pq = w3 * (a2[q] > 0.f ? a2[q] : 0.f);
+        for (int off = 16; off; off >>= 1) pq += __shfl_xor_sync(full, pq, off);
+        if ((u & 31) == 0) red[q * 2 + (u >> 5)] = pq;
+    }
+    __syncthreads();
+    // backward
+    float gw3 = 0.f, gb2 = 0.f, gb3 = 0.f;
+    double lsum = 0.0;
+    float d2[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+        const bool valid = blockIdx.x * S + q < batch;
+        const float out = red[q * 2] + red[q * 2 + 1] + b3;
+        const float err = valid ? out - (tt[q] - mu) * inv_sd : 0.f;
+        lsum += (double) err * err;
         const float dout = 2.f * err / (float) batch;
-        gw3 = fmaf(dout, r2, gw3);
-        if (u == 0) gb3 += dout;
-        const float d2 = a2 > 0.f ? dout * w3 : 0.f;
-        dh2[u] = d2;
-        gb2 += d2;
-        for (int k = 0; k < H; ++k) gW2[u * kH2 + k] = fmaf(d2, h1[k], gW2[u * kH2 + k]);
-        __syncthreads();
-        float s = 0.f;
-        for (int v = 0; v < H; ++v) s = fmaf(dh2[v], W2[v * kH2 + u], s);
-        const float d1 = a1 > 0.f ? s : 0.f;
-        gb1 += d1;
-        for (int j = 0; j < K; ++j) gW1[u * KP + j] = fmaf(d1, xs[j], gW1[u * KP + j]);
-        __syncthreads();
+        gw3 = fmaf(dout, a2[q] > 0.f ? a2[q] : 0.f, gw3);
+        gb3 += dout;
+        d2[q] = a2[q] > 0.f ? dout * w3 : 0.f;
+        gb2 += d2[q];
+        dh2t[u * S + q] = d2[q];
     }
     float *g = gpart + (size_t) blockIdx.x * o.n;
-#pragma unroll 8
-    for (int r = 0; r < H; ++r)
-        for (int c = u; c < K; c += H) g[o.w1 + r * K + c] = gW1[r * KP + c];
-#pragma unroll 8
-    for (int r = 0; r < H; ++r) g[o.w2 + r * H + u] = gW2[r * kH2 + u];
+    // dW2 (u, k) = sum_q d2[q] h1[q][k], stored transposed
+    for (int k = 0; k < H; ++k) {
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < S; ++q) acc = fmaf(d2[q], h1t[k * S + q], acc);
+        g[o.w2 + k * H + u] = acc;
+    }
+    __syncthreads();
+    // back to layer 1: s[q] = sum_v d2[q][v] W2[v][u]
+    float sv[S];
+#pragma unroll
+    for (int q = 0; q < S; ++q) sv[q] = 0.f;
+    for (int v = 0; v < H; ++v) {
+        const float w = W2[v * kH2 + u];
+#pragma unroll
+        for (int q = 0; q < S; ++q) sv[q] = fmaf(w, dh2t[v * S + q], sv[q]);
+    }
+    float gb1 = 0.f;
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+        sv[q] = a1[q] > 0.f ? sv[q] : 0.f;
+        gb1 += sv[q];
+    }
+    // dW1 (u, j) = sum_q d1[q] x[q][j], stored transposed
+    for (int j = 0; j < K; ++j) {
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < S; ++q) acc = fmaf(sv[q], xt[j * S + q], acc);
+        g[o.w1 + j * H + u] = acc;
+    }
     g[o.b1 + u] = gb1;
     g[o.b2 + u] = gb2;
     g[o.w3 + u] = gw3;
@@ -175,17 +210,20 @@ __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params
 }
 
 // grad[i] = sum over the blocks' partials, in block order
-__global__ void k_grad_sum(const float *__restrict__ gpart, int nblocks, int n, float *__restrict__ grad) {
+__global__ void k_grad_sum(const float *__restrict__ gpart, int nblocks, int n, int K, float *__restrict__ grad) {
+    const Offs o = offs(K);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int t = part_index(i, o, K);
         float g = 0.f;
-        for (int b = 0; b < nblocks; ++b) g += gpart[(size_t) b * n + i];
+        for (int b = 0; b < nblocks; ++b) g += gpart[(size_t) b * n + t];
         grad[i] = g;
     }
 }
 
 size_t grad_smem(int K) {
     const int KP = odd_stride(K);
-    return sizeof(float) * (2 * (size_t) H * KP + 2 * (size_t) H * kH2 + (size_t) kSPB * (KP + 1) + 2 * H + 2);
+    return sizeof(float) * ((size_t) H * KP + (size_t) H * kH2 + (size_t) K * kSPB + kSPB + 2 * (size_t) H * kSPB +
+                            2 * kSPB);
 }
 
 // ---- Adam: sum of the partial gradients (block order), update; the last block out records
@@ -195,13 +233,15 @@ __global__ void __launch_bounds__(256) k_adam(float *__restrict__ params, const 
                                               int nblocks, float *__restrict__ m, float *__restrict__ v, int n,
                                               unsigned *__restrict__ step, unsigned *__restrict__ done,
                                               double *__restrict__ loss_acc, float *__restrict__ loss_hist,
-                                              int batch, float lr) {
+                                              int batch, float lr, int K) {
     const unsigned t = *step + 1u;
     const float c1 = 1.f - powf(0.9f, (float) t), c2 = 1.f - powf(0.999f, (float) t);
+    const Offs o = offs(K);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int pi = part_index(i, o, K);
         float g = 0.f;
 #pragma unroll 8
-        for (int b = 0; b < nblocks; ++b) g += gpart[(size_t) b * n + i];
+        for (int b = 0; b < nblocks; ++b) g += gpart[(size_t) b * n + pi];
         const float mi = 0.9f * m[i] + 0.1f * g;
         const float vi = 0.999f * v[i] + 0.001f * g * g;
         m[i] = mi;
@@ -537,7 +577,7 @@ int calibrate_rows_learned(const double *dist, int stride, int offset, double *P
     for (int k = 0; k < kGraphSteps; ++k) {
         k_mlp_grad<<<gblocks, H, gsm, st>>>(params, K, x, target, nh, batch, (float) mu, (float) (1.0 / sd), step,
                                             grad, loss);
-        k_adam<<<ablocks, 256, 0, st>>>(params, grad, gblocks, m, v, o.n, step, done, loss, hist, batch, lr);
+        k_adam<<<ablocks, 256, 0, st>>>(params, grad, gblocks, m, v, o.n, step, done, loss, hist, batch, lr, K);
     }
     cudaError_t ce = cudaStreamEndCapture(st, &graph);
     if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
@@ -630,7 +670,7 @@ int mlp_loss_grad_host(const float *params, int K, const double *dist, const dou
     const size_t gsm = grad_smem(K);
     MCK(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) gsm));
     k_mlp_grad<<<gblocks, H, gsm>>>(dp, K, x, target, nrows, nrows, (float) mu, (float) (1.0 / sd), nullptr, gp, dl);
-    k_grad_sum<<<(o.n + 255) / 256, 256>>>(gp, gblocks, o.n, dg);
+    k_grad_sum<<<(o.n + 255) / 256, 256>>>(gp, gblocks, o.n, K, dg);
     MCK(cudaGetLastError());
     MCK(cudaDeviceSynchronize());
     MCK(cudaMemcpy(grad, dg, sizeof(float) * o.n, cudaMemcpyDeviceToHost));
