@@ -22,7 +22,8 @@ the same steps (`plain_fp64`); the FP32 gradient is compared with the FP64 one a
 starting state (`grad_rel_l2_vs_fp64`) and with the restated reference gradient (oracle/,
 FP64) on the reference's P at that state (`grad_rel_l2_vs_oracle`).  `on_cpu_inputs` times
 the GPU on exactly the CPU leg's P, start state and steps.  `batch` runs the batched form
-(64 jobs, below) and the same jobs one by one.
+(64 jobs, below) and the same jobs one by one; `similarities` times the input-similarity stage
+alone, with the tcgen05 kNN candidate search against the tensor roofline.
 
 reference arm (and the cpu_baseline leg of the gb300 arm, same inputs): the reference's CPU
 path (the C restatement in oracle/, the reference tree is not on the GPU machine) on all host
@@ -424,6 +425,10 @@ def run_gb300(args, world, rank, local):
     batch = None
     if rank == 0 and not args.skip_batch:
         batch = batch_measure(fitsne, args.jobs)
+    sims = None
+    if rank == 0 and not args.skip_batch:
+        sims = similarity_measure(fitsne, N)
+        sims.pop("stage_log", None)
 
     if rank != 0:
         return 0
@@ -445,55 +450,60 @@ def run_gb300(args, world, rank, local):
             "plain_fp64": {"value": fp64_value, "unit": "iters/s", "steps": k64, "speedup": value / fp64_value},
             "grad_rel_l2_vs_fp64": grad_rel, "Z": z32,
             "grad_rel_l2_vs_oracle": grad_vs_oracle["rel_l2"] if grad_vs_oracle else None,
-            "grad_vs_oracle": grad_vs_oracle, "on_cpu_inputs": on_cpu_inputs, "batch": batch,
+            "grad_vs_oracle": grad_vs_oracle, "on_cpu_inputs": on_cpu_inputs, "batch": batch, "similarities": sims,
             "gpu_launches": launches, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e}
     print(json.dumps(line))
     return 0
 
 
-def run_similarities(args, world, rank):
-    """The input-similarity stage alone (kNN + calibration + symmetrisation) on the GPU."""
-    if rank != 0:
-        return 0
-    import fitsne
-    X, _, _ = mixture(args.n)
-    if args.shuffle:  # rows in random order instead of grouped by cluster
-        X = X[np.random.default_rng(11).permutation(args.n)]
+def similarity_measure(fitsne, n, shuffle=False, reps=2):
+    """The input-similarity stage alone on the GPU (kNN + calibration, then symmetrisation),
+    with the tcgen05 candidate search against the tensor roofline."""
+    X, _, _ = mixture(n)
+    if shuffle:  # rows in random order instead of grouped by cluster
+        X = X[np.random.default_rng(11).permutation(n)]
     Xn = X - X.mean(0)
     Xn /= np.abs(Xn).max()
+    had = os.environ.get("FITSNE_TIMING")
     os.environ["FITSNE_TIMING"] = "1"
     times = []
-    for rep in range(1 + args.warmup // 3):
-        with tempfile.TemporaryFile(mode="w+") as log:
-            fd = sys.stderr.fileno()
-            saved = os.dup(fd)
-            os.dup2(log.fileno(), fd)
-            try:
-                t0 = time.perf_counter()
-                row, col, val = fitsne.gaussian_perplexity(Xn, PERPLEXITY, K_NEIGH)
-                t1 = time.perf_counter()
-                fitsne.symmetrize(row, col, val, args.n)
-                t2 = time.perf_counter()
-            finally:
-                os.dup2(saved, fd)
-                os.close(saved)
-            log.seek(0)
-            text = log.read()
-        times.append((t1 - t0, t2 - t1, text))
+    try:
+        for rep in range(reps):
+            with tempfile.TemporaryFile(mode="w+") as log:
+                fd = sys.stderr.fileno()
+                saved = os.dup(fd)
+                os.dup2(log.fileno(), fd)
+                try:
+                    t0 = time.perf_counter()
+                    row, col, val = fitsne.gaussian_perplexity(Xn, PERPLEXITY, K_NEIGH)
+                    t1 = time.perf_counter()
+                    fitsne.symmetrize(row, col, val, n)
+                    t2 = time.perf_counter()
+                finally:
+                    os.dup2(saved, fd)
+                    os.close(saved)
+                log.seek(0)
+                text = log.read()
+            times.append((t1 - t0, t2 - t1, text))
+    finally:
+        if had is None:
+            del os.environ["FITSNE_TIMING"]
+        else:
+            os.environ["FITSNE_TIMING"] = had
     knn_s, sym_s, text = times[-1]
     cand_s = float(text.split("candidates ")[1].split(" s")[0]) if "candidates " in text else None
     kept = float(text.split("tile pairs computed ")[1].split("%")[0]) / 100 if "tile pairs computed " in text else 1.0
     peak, kind = bf16_peak()
     # tensor work issued: per computed (128-query, 64-point) tile pair three BF16 products of
     # K = 64 (D = 50 padded with the folded norm columns)
-    npad = -(-args.n // 128) * 128
+    npad = -(-n // 128) * 128
     flops = kept * (npad / 128) * (npad / 64) * 2.0 * 128 * 64 * 64 * 3
-    dense = 2.0 * args.n * args.n * D_IN
-    line = {"metric": "similarity stage seconds (kNN K=91 + calibration; symmetrisation)", "value": knn_s + sym_s,
-            "unit": "s", "n_gpus": 1, "higher_is_better": False, "data": "synthetic (seeded Gaussian mixture)",
-            "config": {"workload": "N=%d x D=50 Gaussian mixture, perplexity 30, K=90" % args.n,
-                       "row_order": "shuffled" if args.shuffle else "grouped by cluster"},
-            "knn_and_calibration_s": knn_s, "symmetrisation_s": sym_s, "stage_log": text.strip().splitlines(),
+    dense = 2.0 * n * n * D_IN
+    return {"metric": "similarity stage seconds (kNN K=91 + calibration; symmetrisation)", "value": knn_s + sym_s,
+            "unit": "s", "workload": "N=%d x D=50 Gaussian mixture, perplexity 30, K=90" % n,
+            "row_order": "shuffled" if shuffle else "grouped by cluster",
+            "knn_and_calibration_s": knn_s, "symmetrisation_s": sym_s, "candidate_search_s": cand_s,
+            "stage_log": text.strip().splitlines(),
             "roofline": {"bound": "tensor", "kernel": "tcgen05 kNN candidate search (k_knn_tc)",
                          "achieved": flops / cand_s / 1e12 if cand_s else None, "peak": peak, "peak_kind": kind,
                          "unit": "TFLOP/s", "frac": flops / cand_s / 1e12 / peak if cand_s else None,
@@ -502,6 +512,18 @@ def run_similarities(args, world, rank):
                          "note": "tensor flops issued (computed tile pairs x 128 x 64 x 64 x 2 x 3 split products) "
                                  "over the host-clock time of the candidate phase (ordering, bounds, BF16 planes, "
                                  "kernel); dense_equivalent = 2 N^2 D over the same time"}}
+
+
+def run_similarities(args, world, rank):
+    """The input-similarity stage alone (kNN + calibration + symmetrisation) on the GPU."""
+    if rank != 0:
+        return 0
+    import fitsne
+    m = similarity_measure(fitsne, args.n, args.shuffle, 1 + args.warmup // 3)
+    line = {"metric": m.pop("metric"), "value": m.pop("value"), "unit": m.pop("unit"), "n_gpus": 1,
+            "higher_is_better": False, "data": "synthetic (seeded Gaussian mixture)",
+            "config": {"workload": m.pop("workload"), "row_order": m.pop("row_order")}}
+    line.update(m)
     print(json.dumps(line))
     return 0
 
