@@ -197,13 +197,25 @@ int Embedding<T>::check_symmetric() {
     return build_tiles();
 }
 
+// The tiled form pays a build (a radix sort of the upper entries) at set-up and after every
+// renumbering; it is built only where it can win: up to kTilesMaxN points (measured: it wins
+// at 50,000 points, ties at 200,000 and loses at 1,000,000), or when FITSNE_ATTR_SHAPE asks for
+// it.
+template <typename T>
+bool Embedding<T>::tiles_wanted() const {
+    if (!sym_ok_) return false;
+    if (N_ <= kTilesMaxN) return true;
+    const char *fixed = std::getenv("FITSNE_ATTR_SHAPE");
+    return fixed && *fixed && std::atoi(fixed) == kAttrTilesShape;
+}
+
 // Records of the upper entries sorted by tile (A, B) of 4,096-point blocks, row order kept
 // within a tile (stable radix sort on the tile key), and the tiles' first records.  Rebuilt
 // after every renumbering: the tiles follow the point order.
 template <typename T>
 int Embedding<T>::build_tiles() {
     tiles_ok_ = false;
-    if (!sym_ok_) return 0;
+    if (!tiles_wanted()) return 0;
     const int nblk = tile_blocks(N_);
     const size_t nkeys = (size_t) nblk * nblk;
     if (nkeys >= (1ull << 30)) return 0;

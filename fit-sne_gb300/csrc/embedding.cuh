@@ -199,6 +199,8 @@ class Embedding {
     float *acc_ = nullptr;
     int check_symmetric();  // sets sym_ok_ (FP32 form, FITSNE_ATTR_SYM unset or 1), builds the tiles
     int build_tiles();      // from the current CSR (after every renumbering)
+    static constexpr int kTilesMaxN = 262144;
+    bool tiles_wanted() const;
     // the attraction + update of the given shape (either form)
     cudaError_t attr_call(const T *Yin, T *Yout, T *uY, T *gains, T *dC, const UpdateParams &p, int shape);
     int tune_phase_ = 1;   // phase of the current iteration (tune_phase)
