@@ -79,6 +79,14 @@ __global__ void k_scale(double *__restrict__ X, size_t n, const unsigned long lo
 // FP64 exactly as the reference does.  The betas visited, the number of steps and P (the
 // FP64 row of the last evaluation, which is always an FP64 one when the bisection
 // converges) are therefore the reference's, bit for bit.
+//
+// The FP64 pipe issues a warp instruction at the same cost however many of its lanes are
+// active, and a row needs its FP64 steps (1.5 on average, at most about 3) near the end of
+// its bisection, at a step index that differs from row to row.  Taken where they fall, a
+// warp's FP64 steps would run one after another with a lane or two active each.  So the
+// warp's rows advance in rounds: each row takes FP32 steps until its next step needs FP64,
+// then every row that needs one takes it together.  Each row's sequence of steps is
+// unchanged, only the interleaving between rows differs.
 
 // One bisection step in FP32 (screen_value): +1 when H(beta) - logU > tol for certain, -1
 // when it is below -tol for certain, 0 when the FP32 value cannot decide.  The shifted form
@@ -99,42 +107,24 @@ __device__ __forceinline__ int screen_step(const float *__restrict__ s, int sstr
 
 // Calibrates one row.  s (may be null: FP64 steps only) is the row's FP32 shifted copy for
 // screen_step; d0 the row's smallest distance.  Writes the normalised row p and returns the
-// beta the reference's loop returns.
+// beta the reference's loop returns.  Called by every lane of the warp together (the FP64
+// rounds are warp-wide); a lane without a row passes active = false and touches no memory.
 __device__ double calibrate_row(const double *__restrict__ d, double *__restrict__ p, int K, double perplexity,
-                                double sigma, int *evals = nullptr, const float *__restrict__ s = nullptr,
+                                double sigma, bool active, int *evals = nullptr, const float *__restrict__ s = nullptr,
                                 int sstride = 0, double d0 = 0.0) {
     if (perplexity > 0) {
         double min_beta = -DBL_MAX, max_beta = DBL_MAX;
         const double tol = 1e-5;
         const double logU = log(perplexity);
-        bool found = false;
+        bool found = !active;
         int iter = 0;
         double beta = 1.0;
         double beta_eval = beta;
         bool last_fp64 = false;  // p holds exp(-beta_eval d) and last_sum their sum
         double last_sum = DBL_MIN;
-        while (!found && iter < 200) {
-            beta_eval = beta;
-            int dir = s ? screen_step(s, sstride, K, beta, d0, logU, tol) : 0;
-            last_fp64 = (dir == 0);
-            if (dir == 0) {
-                double sum_P = DBL_MIN, H = 0.0;
-                for (int m = 0; m < K; ++m) {
-                    const double e = exp(-beta * d[m]);
-                    p[m] = e;
-                    sum_P += e;
-                    H += beta * (d[m] * e);
-                }
-                H = (H / sum_P) + log(sum_P);
-                last_sum = sum_P;
-                const double Hdiff = H - logU;
-                if (Hdiff < tol && -Hdiff < tol)
-                    found = true;
-                else
-                    dir = Hdiff > 0 ? 1 : -1;
-            }
-            if (found) {
-            } else if (dir > 0) {
+        // the bracket moves up (dir > 0: H too large) or down
+        auto move = [&](int dir) {
+            if (dir > 0) {
                 min_beta = beta;
                 if (max_beta == DBL_MAX || max_beta == -DBL_MAX)
                     beta *= 2.0;
@@ -147,8 +137,45 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
                 else
                     beta = (beta + min_beta) / 2.0;
             }
-            iter++;
+        };
+        while (true) {
+            // FP32 steps while they decide; stop at the first step that needs FP64
+            bool need64 = false;
+            while (!found && iter < 200) {
+                beta_eval = beta;
+                const int dir = s ? screen_step(s, sstride, K, beta, d0, logU, tol) : 0;
+                if (dir == 0) {
+                    need64 = true;
+                    break;
+                }
+                last_fp64 = false;
+                move(dir);
+                iter++;
+            }
+            // one round: the FP64 step of every row of the warp that needs one
+            if (!__any_sync(0xffffffffu, need64)) break;
+            if (need64) {
+                double sum_P = DBL_MIN, H = 0.0;
+                for (int m = 0; m < K; ++m) {
+                    const double e = exp(-beta * d[m]);
+                    p[m] = e;
+                    sum_P += e;
+                    H += beta * (d[m] * e);
+                }
+                H = (H / sum_P) + log(sum_P);
+                last_sum = sum_P;
+                last_fp64 = true;
+                const double Hdiff = H - logU;
+                if (Hdiff < tol && -Hdiff < tol)
+                    found = true;
+                else
+                    move(Hdiff > 0 ? 1 : -1);
+                iter++;
+            }
+            // the next round's FP32 steps start with the whole warp together
+            __syncwarp();
         }
+        if (!active) return beta;
         if (evals) *evals = iter;
         // P of the reference is the row evaluated at beta_eval; the returned beta is the
         // updated one when the loop ran out of iterations (as in the reference)
@@ -163,6 +190,7 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
         return beta;
     }
     const double beta_eval = 1 / (2 * sigma * sigma);
+    if (!active) return beta_eval;
     double sum_P = DBL_MIN;
     for (int m = 0; m < K; ++m) {
         p[m] = exp(-beta_eval * d[m]);
@@ -175,37 +203,44 @@ __device__ double calibrate_row(const double *__restrict__ d, double *__restrict
 // Rows of the block in shared memory as FP32 shifted distances, one column per thread
 // ([m][thread]: the lanes of a warp read consecutive words), when the launch provides the
 // space (stage = 1); the FP64 distances stay in global memory (read only by FP64 steps).
+// The block size is a multiple of 32, and lanes past the last row stay in their warp.
 __global__ void k_calibrate(const double *__restrict__ dist, int stride, int offset, double *__restrict__ P,
                             double *__restrict__ tmp, int nrows, int K, double perplexity, double sigma,
                             const double *__restrict__ list, int list_len, double *__restrict__ beta_out,
                             int *__restrict__ evals_out, int stage) {
     extern __shared__ float s_shift[];
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nrows) return;
-    const double *d = dist + (size_t) r * stride + offset;
-    double *p = P + (size_t) r * K;
+    const bool active = r < nrows;
+    const int rr = active ? r : 0;
+    const double *d = dist + (size_t) rr * stride + offset;
+    double *p = P + (size_t) rr * K;
     const float *s = nullptr;
     double d0 = 0.0;
     if (stage && perplexity >= 0) {
-        d0 = d[0];
-        for (int m = 1; m < K; ++m) d0 = fmin(d0, d[m]);
         float *w = s_shift + threadIdx.x;
-        for (int m = 0; m < K; ++m) w[(size_t) m * blockDim.x] = (float) (d[m] - d0);
+        if (active) {
+            d0 = d[0];
+            for (int m = 1; m < K; ++m) d0 = fmin(d0, d[m]);
+            for (int m = 0; m < K; ++m) w[(size_t) m * blockDim.x] = (float) (d[m] - d0);
+        }
         s = w;
     }
     double beta;
     int evals = 0;
     if (perplexity != 0) {
-        beta = calibrate_row(d, p, K, perplexity, sigma, &evals, s, blockDim.x, d0);
+        beta = calibrate_row(d, p, K, perplexity, sigma, active, &evals, s, blockDim.x, d0);
     } else {
-        double *t = tmp + (size_t) r * K;
-        beta = calibrate_row(d, p, K, list[0], sigma, &evals, s, blockDim.x, d0);
+        double *t = tmp + (size_t) rr * K;
+        beta = calibrate_row(d, p, K, list[0], sigma, active, &evals, s, blockDim.x, d0);
         for (int m = 1; m < list_len; ++m) {
-            beta = calibrate_row(d, t, K, list[m], sigma, nullptr, s, blockDim.x, d0);
-            for (int i = 0; i < K; ++i) p[i] += t[i];
+            beta = calibrate_row(d, t, K, list[m], sigma, active, nullptr, s, blockDim.x, d0);
+            if (active)
+                for (int i = 0; i < K; ++i) p[i] += t[i];
         }
-        for (int i = 0; i < K; ++i) p[i] /= list_len;
+        if (active)
+            for (int i = 0; i < K; ++i) p[i] /= list_len;
     }
+    if (!active) return;
     if (beta_out) beta_out[r] = beta;
     if (evals_out) evals_out[r] = evals;
 }
