@@ -349,6 +349,15 @@ void print_knn_stats(int K, const KnnStats &ks, double total_s) {
         std::fprintf(stderr, ", locality order %.3f s, tile pairs computed %.1f%%, per query %.0f columns kept, %.0f inserts",
                      ks.tc.s_order, 100.0 * ks.tc.tiles_kept, ks.tc.cols_per_query, ks.tc.inserts_per_query);
     std::fprintf(stderr, "\n");
+    if (ks.tensor_cores)
+        std::fprintf(stderr,
+                     "[fitsne] kNN tcgen05 pipeline (shares of each role's time): producer waiting for a stage "
+                     "%.1f%%, MMA waiting for operands %.1f%% / for an accumulator %.1f%%, epilogue waiting for an "
+                     "accumulator %.1f%%, in threshold stash and inserts %.1f%% (%.2f insert-loop iterations a tile, "
+                     "%.0f cycles each)\n",
+                     100.0 * ks.tc.producer_stage_wait, 100.0 * ks.tc.mma_data_wait, 100.0 * ks.tc.mma_acc_wait,
+                     100.0 * ks.tc.epilogue_acc_wait, 100.0 * ks.tc.epilogue_inserts, ks.tc.insert_iters_per_tile,
+                     ks.tc.cycles_per_insert_iter);
 }
 
 int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist, cudaStream_t st, KnnStats *stats,

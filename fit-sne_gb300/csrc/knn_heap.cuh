@@ -76,6 +76,34 @@ struct Heap4 {
         at(pos) = HeapEntry{v, id};
     }
 
+    // sift_down from the root without branches: the new root (v, id) of a heap of n <= 341
+    // entries (four levels of children) goes down four fixed levels, children past n and
+    // every level below the one where the entry stops predicated off, with sift_down's choice
+    // of child.  The lanes of a warp stay together whatever depth their entries reach.
+    KNN_HEAP_HD void replace_top(int n, float v, uint32_t id) const {
+        const HeapEntry lowest{-3.402823466e38f, 0u};  // below every distance: never moves up
+        int pos = 0;
+        bool go = true;
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int c = 4 * pos + 1;
+            const HeapEntry e0 = (go && c < n) ? at(c) : lowest;
+            const HeapEntry e1 = (go && c + 1 < n) ? at(c + 1) : lowest;
+            const HeapEntry e2 = (go && c + 2 < n) ? at(c + 2) : lowest;
+            const HeapEntry e3 = (go && c + 3 < n) ? at(c + 3) : lowest;
+            const bool b01 = e1.d > e0.d, b23 = e3.d > e2.d;
+            const HeapEntry m01 = b01 ? e1 : e0, m23 = b23 ? e3 : e2;
+            const int i01 = b01 ? c + 1 : c, i23 = b23 ? c + 3 : c + 2;
+            const bool b = m23.d > m01.d;
+            const HeapEntry m = b ? m23 : m01;
+            const bool mv = m.d > v;
+            if (mv) at(pos) = m;
+            pos = mv ? (b ? i23 : i01) : pos;
+            go = mv;
+        }
+        at(pos) = HeapEntry{v, id};
+    }
+
     // sorts the n entries ascending in place (heap sort)
     KNN_HEAP_HD void sort_ascending(int n) const {
         for (int end = n - 1; end > 0; --end) {

@@ -62,9 +62,18 @@ constexpr uint32_t kSbMask = kMaxSB - 1;
 constexpr int kTmemCols = 2 * BN;                  // two accumulators
 constexpr int kStashOff = 2 * kATileBytes + kStages * 2 * kBTileBytes;  // 80 KB
 constexpr int kHeapOff = kStashOff + 32 * BM * 4;                       // + 16 KB stash
-constexpr size_t kSmemBytes = (size_t) kHeapOff + (size_t) kMaxTcCandidates * BM * 8 + 1024;
+constexpr int kQueue = 5;  // candidates queued per query row between heap flushes
+constexpr int kQueueOff = kHeapOff + kMaxTcCandidates * BM * 8;          // + 120 KB heaps
+constexpr size_t kSmemBytes = (size_t) kQueueOff + (size_t) kQueue * BM * 8 + 1024;  // + 5 KB queues
 constexpr long long kWaitCycles = 2000000000LL;  // about one second
-static_assert(kSmemBytes <= 232448, "shared memory budget");
+// counters: kept tiles, columns past the threshold test, heap inserts, producer cycles waiting
+// for a free stage, producer cycles, MMA cycles waiting for data, MMA cycles waiting for an
+// accumulator, epilogue cycles waiting for an accumulator, epilogue cycles in the threshold
+// stash and inserts, epilogue cycles, insert-loop iterations (warp level), tiles (per warp)
+constexpr int kNumCounters = 12;
+// with the kernel's 4.5 KB of static shared memory, within the 227 KB a block may use
+static_assert(kSmemBytes + 4608 <= 232448, "shared memory budget");
+static_assert(kMaxTcCandidates <= 341, "Heap4::replace_top covers four levels of children");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
 
@@ -215,6 +224,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint8_t *sB = base + 2 * kATileBytes;  // stage s: hi at s*2*kBTileBytes, lo after it
     float *stash = reinterpret_cast<float *>(base + kStashOff);  // [32 columns][BM rows]
     HeapEntry *heaps = reinterpret_cast<HeapEntry *>(base + kHeapOff);  // entry e of row r at e*BM + r
+    HeapEntry *queues = reinterpret_cast<HeapEntry *>(base + kQueueOff);  // entry k of row r at k*BM + r
 
     const int nQT = Npad / BM;
     const int nRT = Npad / BN;
@@ -255,7 +265,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         long long g = 0;  // stages filled so far (tiles and end markers)
         long long last_g[kStages];
         for (int s = 0; s < kStages; ++s) last_g[s] = -1;
-        unsigned long long kept = 0;
+        unsigned long long kept = 0, t_stage_wait = 0;
+        const long long t_begin = clock64();
         for (int qt = blockIdx.x; qt < nQT && ok; qt += gridDim.x, ++j) {
             if (lane == 0) {
                 ok = mbar_wait(&bar_a_empty, (j & 1) ^ 1, &abort_flag);
@@ -306,7 +317,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int s = (int) (g % kStages);
                 const uint32_t ph = (uint32_t) ((g / kStages) & 1);
                 if (lane == 0) {
+                    const long long tw = clock64();
                     ok = mbar_wait(&bar_b_empty[s], ph ^ 1, &abort_flag);
+                    t_stage_wait += (unsigned long long) (clock64() - tw);
                     if (ok) {
                         stage_tile[s] = rt;
                         // the stage's latest phase (a copy or a marker): the final drain waits on
@@ -378,6 +391,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int s = 0; s < kStages; ++s)
                 if (last_g[s] >= 0) mbar_drain(&bar_b_full[s], (uint32_t) ((last_g[s] / kStages) & 1), &abort_flag);
             atomicAdd(&counters[0], kept);
+            atomicAdd(&counters[3], t_stage_wait);
+            atomicAdd(&counters[4], (unsigned long long) (clock64() - t_begin));
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -386,6 +401,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             int j = 0;
             bool ok = true;
             long long g = 0, a = 0;  // stages consumed, accumulators handed over
+            unsigned long long t_data = 0, t_acc = 0;
             for (int qt = blockIdx.x; qt < nQT && ok; qt += gridDim.x, ++j) {
                 if (!(ok = mbar_wait(&bar_a_full, j & 1, &abort_flag))) break;
                 while (true) {
@@ -393,8 +409,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint32_t ph = (uint32_t) ((g / kStages) & 1);
                     const int b = (int) (a & 1);
                     const uint32_t phb = (uint32_t) ((a >> 1) & 1);
+                    const long long t0 = clock64();
                     if (!(ok = mbar_wait(&bar_b_full[s], ph, &abort_flag))) break;
+                    const long long t1 = clock64();
                     if (!(ok = mbar_wait(&bar_acc_empty[b], phb ^ 1, &abort_flag))) break;
+                    t_data += (unsigned long long) (t1 - t0);
+                    t_acc += (unsigned long long) (clock64() - t1);
                     const int rt = stage_tile[s];
                     acc_tile[b] = rt;
                     if (rt >= 0) {
@@ -423,6 +443,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
                 if (ok) mma_commit(&bar_a_empty);
             }
+            atomicAdd(&counters[5], t_data);
+            atomicAdd(&counters[6], t_acc);
             // all issued MMAs retire before TMEM is released
             mma_commit(&bar_done);
             mbar_drain(&bar_done, 0u, &abort_flag);
@@ -433,22 +455,52 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int row = quarter * 32 + lane;
         const Heap4<BM> hp{heaps + row};
         float *my_stash = stash + row;
+        HeapEntry *my_queue = queues + row;
         int j = 0;
         bool ok = true;
         long long a = 0;  // accumulators received
         unsigned ncols = 0, nins = 0;  // columns through the threshold test, heap insertions
+        unsigned long long t_wait = 0, t_ins = 0, n_iter = 0, n_tiles = 0;
+        const long long t_begin = clock64();
         for (int qt = blockIdx.x; qt < nQT && ok; qt += gridDim.x, ++j) {
             const int q = qt * BM + row;
             const bool qvalid = q < N;
             const float nq = qvalid ? qnorm2[q] : 0.f;
             int n = 0;
             float thr = qvalid ? FLT_MAX : -FLT_MAX;  // rows past N keep nothing
+            int qn = 0;  // queued candidates of this row
+            // one candidate into the row's heap (thr: the heap's top once it holds C)
+            auto insert = [&](float d2, uint32_t col) {
+                if (d2 < thr) {
+                    ++nins;
+                    if (n < C) {
+                        hp.push(n, d2, col);
+                        if (n == C) thr = hp.top();
+                    } else {
+                        hp.replace_top(n, d2, col);
+                        thr = hp.top();
+                    }
+                }
+            };
+            // every row's queued candidates into its heap, the warp's lanes side by side
+            auto flush = [&]() {
+                const int m = (int) __reduce_max_sync(0xffffffffu, (unsigned) qn);
+                n_iter += (unsigned long long) m;
+                for (int k = 0; k < m; ++k)
+                    if (k < qn) {
+                        const HeapEntry e = my_queue[k * BM];
+                        insert(e.d, e.i);
+                    }
+                qn = 0;
+            };
             while (true) {
                 const int b = (int) (a & 1);
                 const uint32_t phb = (uint32_t) ((a >> 1) & 1);
                 ++a;
                 // warp-uniform outcome: the TMEM loads below need all 32 lanes
+                const long long tacc = clock64();
                 if (!(ok = __all_sync(0xffffffffu, mbar_wait(&bar_acc_full[b], phb, &abort_flag)))) break;
+                t_wait += (unsigned long long) (clock64() - tacc);
                 const int rt = acc_tile[b];
                 if (rt < 0) {  // end of this query tile
                     __syncwarp();
@@ -494,39 +546,55 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint32_t lim = nv >= 32 ? 0xffffffffu : (nv <= 0 ? 0u : ((1u << nv) - 1u));
                     mk[h] = ((q0 | q1) | (q2 | q3)) & lim;
                 }
+                const long long ti = clock64();
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     uint32_t mask = mk[h];
                     if (__any_sync(0xffffffffu, mask != 0u)) {
                         // stash the half (entry jj of row r at jj*BM + r: conflict-free), then each
-                        // lane inserts its own kept columns
+                        // lane walks its own kept columns
 #pragma unroll
                         for (int jj = 0; jj < 32; ++jj) my_stash[jj * BM] = __uint_as_float(v[32 * h + jj]);
                         const int colbase = tilebase + 32 * h;
-                        while (mask) {
-                            const int jj = __ffs(mask) - 1;
-                            mask &= mask - 1;
-                            const float d2 = fmaf(-2.f, my_stash[jj * BM], nq);
-                            ++ncols;
-                            if (d2 < thr) {
-                                ++nins;
-                                if (n < C) {
-                                    hp.push(n, d2, (uint32_t) (colbase + jj));
-                                    if (n == C) thr = hp.top();
-                                } else {
-                                    hp.sift_down(n, 0, d2, (uint32_t) (colbase + jj));
-                                    thr = hp.top();
+                        const int pc = __popc(mask);
+                        // a heap insert is a chain of dependent shared-memory round trips that the
+                        // warp runs once per kept column of its busiest lane; so the candidates that
+                        // pass the threshold are queued per row, and the queues go into the heaps
+                        // together when one of them would overflow (the threshold lags until then,
+                        // which only queues more candidates: each is tested again at the flush)
+                        if (__any_sync(0xffffffffu, qn + pc > kQueue)) flush();
+                        if (__any_sync(0xffffffffu, pc > kQueue)) {
+                            // more kept columns than a queue holds (lists still filling): straight in
+                            n_iter += (unsigned long long) __reduce_max_sync(0xffffffffu, (unsigned) pc);
+                            while (mask) {
+                                const int jj = __ffs(mask) - 1;
+                                mask &= mask - 1;
+                                ++ncols;
+                                insert(fmaf(-2.f, my_stash[jj * BM], nq), (uint32_t) (colbase + jj));
+                            }
+                        } else {
+                            while (mask) {
+                                const int jj = __ffs(mask) - 1;
+                                mask &= mask - 1;
+                                ++ncols;
+                                const float d2 = fmaf(-2.f, my_stash[jj * BM], nq);
+                                if (d2 < thr) {
+                                    my_queue[qn * BM] = HeapEntry{d2, (uint32_t) (colbase + jj)};
+                                    ++qn;
                                 }
                             }
                         }
                         __syncwarp();
                     }
                 }
+                t_ins += (unsigned long long) (clock64() - ti);
+                ++n_tiles;
                 // publish this warp's largest threshold for the producer's tile skipping
                 const uint32_t tw = __reduce_max_sync(0xffffffffu, __float_as_uint(fmaxf(thr, 0.f)));
                 if (lane == 0) warp_thr[quarter] = ((unsigned long long) (uint32_t) j << 32) | tw;
             }
             if (!ok) break;
+            flush();
             if (qvalid) {
                 hp.sort_ascending(n);
                 // rows and indices back to the caller's numbering
@@ -542,6 +610,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             atomicAdd(&counters[1], (unsigned long long) cs);
             atomicAdd(&counters[2], (unsigned long long) is);
+            atomicAdd(&counters[7], t_wait);
+            atomicAdd(&counters[8], t_ins);
+            atomicAdd(&counters[9], (unsigned long long) (clock64() - t_begin));
+            atomicAdd(&counters[10], n_iter);
+            atomicAdd(&counters[11], n_tiles);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -857,7 +930,7 @@ int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, flo
         (e = cudaMalloc(&qn, sizeof(float) * Npad)) != cudaSuccess ||
         (e = cudaMalloc(&bounds, sizeof(float) * nb)) != cudaSuccess ||
         (e = cudaMalloc(&derr, sizeof(int))) != cudaSuccess ||
-        (e = cudaMalloc(&dcount, 3 * sizeof(unsigned long long))) != cudaSuccess) {
+        (e = cudaMalloc(&dcount, kNumCounters * sizeof(unsigned long long))) != cudaSuccess) {
         err = std::string("knn tc allocation: ") + cudaGetErrorString(e);
         cleanup();
         return -10;
@@ -866,7 +939,7 @@ int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, flo
     float *rcent = bounds, *qcent = rcent + (size_t) nRT * KD, *sbcent = qcent + (size_t) nQT * KD;
     float *rrad = sbcent + (size_t) nSB * KD, *qrad = rrad + nRT, *sbrad = qrad + nQT;
     cudaMemsetAsync(derr, 0, sizeof(int), st);
-    cudaMemsetAsync(dcount, 0, 3 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(dcount, 0, kNumCounters * sizeof(unsigned long long), st);
     k_tc_prep<<<2048, 256, 0, st>>>(Xd, perm, N, D, Npad, qhi, qlo, rhi, rlo, qn);
     k_tile_bounds<<<nRT, 256, 0, st>>>(Xd, perm, N, D, BN, nRT, rcent, rrad);
     k_tile_bounds<<<nQT, 256, 0, st>>>(Xd, perm, N, D, BM, nQT, qcent, qrad);
@@ -894,7 +967,7 @@ int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, flo
     k_knn_tc<<<grid, kThreads, kSmemBytes, st>>>(m_qhi, m_qlo, m_rhi, m_rlo, qn, N, Npad, D, C, SBT, perm, rcent, rrad, sbcent, sbrad,
                                                  qcent, qrad, errm, cand_d, cand_i, derr, dcount);
     int herr = 0;
-    unsigned long long hc[3] = {0, 0, 0};
+    unsigned long long hc[kNumCounters] = {};
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hc, dcount, sizeof(hc), cudaMemcpyDeviceToHost, st);
@@ -903,6 +976,16 @@ int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, flo
         stats->tiles_kept = (double) hc[0] / ((double) nQT * nRT);
         stats->cols_per_query = (double) hc[1] / N;
         stats->inserts_per_query = (double) hc[2] / N;
+        // shares of each role's own clock: the producer's (one warp per CTA), the MMA
+        // issuer's (one thread), the epilogue's (four warps)
+        const double tp = hc[4] > 0 ? (double) hc[4] : 1.0, te = hc[9] > 0 ? (double) hc[9] : 1.0;
+        stats->producer_stage_wait = (double) hc[3] / tp;
+        stats->mma_data_wait = (double) hc[5] / tp;
+        stats->mma_acc_wait = (double) hc[6] / tp;
+        stats->epilogue_acc_wait = (double) hc[7] / te;
+        stats->epilogue_inserts = (double) hc[8] / te;
+        stats->insert_iters_per_tile = hc[11] > 0 ? (double) hc[10] / (double) hc[11] : 0.0;
+        stats->cycles_per_insert_iter = hc[10] > 0 ? (double) hc[8] / (double) hc[10] : 0.0;
     }
     cleanup();
     if (e != cudaSuccess) {

@@ -16,6 +16,12 @@ struct KnnTcStats {
     double cols_per_query = 0;       // columns that passed a query's threshold test, per query
     double inserts_per_query = 0;    // heap insertions (fills and replacements) per query
     double s_order = 0;              // host-clock seconds of the locality order
+    // shares of the kernel's time (each role's own clock): the TMA producer waiting for a free
+    // stage, the MMA issuer waiting for operands / for a free accumulator, the epilogue warps
+    // waiting for a full accumulator / walking their kept columns into the heaps
+    double producer_stage_wait = 0, mma_data_wait = 0, mma_acc_wait = 0;
+    double epilogue_acc_wait = 0, epilogue_inserts = 0;
+    double insert_iters_per_tile = 0, cycles_per_insert_iter = 0;  // epilogue warp level
 };
 
 // True when the device is a Blackwell (cc 10.x) part, the driver exposes the tensor-map
