@@ -20,16 +20,19 @@
 //               and skip the tiles that cannot hold a candidate; the walk ends at the first
 //               superblock too far away, and an end-marker stage (tile index -1) closes the
 //               query tile
-//   warp 1      allocates 128 TMEM columns (two 128 x 64 FP32 accumulators) and issues
-//               the tcgen05.mma (M = 128, N = 64, K = 16) from one thread; tcgen05.commit
+//   warp 1      allocates 256 TMEM columns (a ring of four 128 x 64 FP32 accumulators, so
+//               that the MMAs run up to four tiles ahead of the epilogue) and issues the
+//               tcgen05.mma (M = 128, N = 64, K = 16) from one thread; tcgen05.commit
 //               releases the shared-memory stage and hands the accumulator to the epilogue
 //   warps 2..5  epilogue: one tcgen05.ld of the whole 64-column tile for their 32 TMEM lanes
 //               (= 32 queries), after which the accumulator is handed back to the MMA warp;
 //               threshold test into per-thread bit masks (four independent chains per 32
-//               columns); when a lane of the warp keeps a column, the 32-column half goes to
-//               a shared-memory stash and every lane walks its own mask into its per-query
-//               4-ary max-heap of the C best (shared memory, knn_heap.cuh), so the lanes'
-//               heap updates run side by side and overlap the next MMAs
+//               columns); when a lane of the warp keeps a column, that 32-column half of the
+//               tile goes to a shared-memory stash and every lane walks its own mask: the
+//               columns below its threshold go to its row's queue, and the queues go into the
+//               per-query 4-ary max-heaps of the C best (shared memory, knn_heap.cuh)
+//               together, when one of them would overflow, so the lanes' heap updates run
+//               side by side and overlap the next MMAs
 // Every mbarrier wait gives up after about a second, sets an error flag, and the CTA
 // drains its own in-flight work, frees TMEM and returns.
 #include <cuda.h>
@@ -59,10 +62,14 @@ constexpr int kBTileBytes = BN * KD * 2;           // 8 KB per plane
 constexpr int kStages = 3;
 constexpr int kMaxSB = 1024;                       // superblocks per query tile's ordering
 constexpr uint32_t kSbMask = kMaxSB - 1;
-constexpr int kTmemCols = 2 * BN;                  // two accumulators
+constexpr int kAccs = 4;                           // TMEM accumulators in the MMA -> epilogue ring
+constexpr int kTmemCols = kAccs * BN;
 constexpr int kStashOff = 2 * kATileBytes + kStages * 2 * kBTileBytes;  // 80 KB
-constexpr int kHeapOff = kStashOff + 32 * BM * 4;                       // + 16 KB stash
-constexpr int kQueue = 5;  // candidates queued per query row between heap flushes
+constexpr int kStashCols = 32;  // columns of a tile stashed at a time: one half
+constexpr int kHeapOff = kStashOff + kStashCols * BM * 4;               // + 16 KB stash
+// candidates queued per query row between heap flushes (13 with 16-column stashes measured
+// slower: a flush comes when any lane's queue fills, so longer queues save few flush rounds)
+constexpr int kQueue = 5;
 constexpr int kQueueOff = kHeapOff + kMaxTcCandidates * BM * 8;          // + 120 KB heaps
 constexpr size_t kSmemBytes = (size_t) kQueueOff + (size_t) kQueue * BM * 8 + 1024;  // + 5 KB queues
 constexpr long long kWaitCycles = 2000000000LL;  // about one second
@@ -205,12 +212,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t bar_a_full, bar_a_empty, bar_done;
     __shared__ __align__(8) uint64_t bar_b_full[kStages], bar_b_empty[kStages];
-    __shared__ __align__(8) uint64_t bar_acc_full[2], bar_acc_empty[2];
+    __shared__ __align__(8) uint64_t bar_acc_full[kAccs], bar_acc_empty[kAccs];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
     // reference tile of each stage / accumulator (-1: end of the query tile)
     __shared__ volatile int stage_tile[kStages];
-    __shared__ volatile int acc_tile[2];
+    __shared__ volatile int acc_tile[kAccs];
     // per epilogue warp: (query-tile sequence number << 32) | bits of its largest threshold
     __shared__ volatile unsigned long long warp_thr[4];
     __shared__ float qc_s[KD];  // producer: centre of the current query tile
@@ -222,7 +229,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint8_t *sA_hi = base;
     uint8_t *sA_lo = base + kATileBytes;
     uint8_t *sB = base + 2 * kATileBytes;  // stage s: hi at s*2*kBTileBytes, lo after it
-    float *stash = reinterpret_cast<float *>(base + kStashOff);  // [32 columns][BM rows]
+    float *stash = reinterpret_cast<float *>(base + kStashOff);  // [kStashCols columns][BM rows]
     HeapEntry *heaps = reinterpret_cast<HeapEntry *>(base + kHeapOff);  // entry e of row r at e*BM + r
     HeapEntry *queues = reinterpret_cast<HeapEntry *>(base + kQueueOff);  // entry k of row r at k*BM + r
 
@@ -239,7 +246,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(&bar_b_full[s], 1);
             mbar_init(&bar_b_empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kAccs; ++b) {
             mbar_init(&bar_acc_full[b], 2);  // the MMA commit + the issuer's release of acc_tile
             mbar_init(&bar_acc_empty[b], 4);
         }
@@ -407,8 +414,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 while (true) {
                     const int s = (int) (g % kStages);
                     const uint32_t ph = (uint32_t) ((g / kStages) & 1);
-                    const int b = (int) (a & 1);
-                    const uint32_t phb = (uint32_t) ((a >> 1) & 1);
+                    const int b = (int) (a % kAccs);
+                    const uint32_t phb = (uint32_t) ((a / kAccs) & 1);
                     const long long t0 = clock64();
                     if (!(ok = mbar_wait(&bar_b_full[s], ph, &abort_flag))) break;
                     const long long t1 = clock64();
@@ -494,8 +501,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 qn = 0;
             };
             while (true) {
-                const int b = (int) (a & 1);
-                const uint32_t phb = (uint32_t) ((a >> 1) & 1);
+                const int b = (int) (a % kAccs);
+                const uint32_t phb = (uint32_t) ((a / kAccs) & 1);
                 ++a;
                 // warp-uniform outcome: the TMEM loads below need all 32 lanes
                 const long long tacc = clock64();
@@ -551,11 +558,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int h = 0; h < 2; ++h) {
                     uint32_t mask = mk[h];
                     if (__any_sync(0xffffffffu, mask != 0u)) {
-                        // stash the half (entry jj of row r at jj*BM + r: conflict-free), then each
+                        // stash the columns (entry jj of row r at jj*BM + r: conflict-free), then each
                         // lane walks its own kept columns
 #pragma unroll
-                        for (int jj = 0; jj < 32; ++jj) my_stash[jj * BM] = __uint_as_float(v[32 * h + jj]);
-                        const int colbase = tilebase + 32 * h;
+                        for (int jj = 0; jj < kStashCols; ++jj)
+                            my_stash[jj * BM] = __uint_as_float(v[kStashCols * h + jj]);
+                        const int colbase = tilebase + kStashCols * h;
                         const int pc = __popc(mask);
                         // a heap insert is a chain of dependent shared-memory round trips that the
                         // warp runs once per kept column of its busiest lane; so the candidates that
