@@ -56,6 +56,7 @@ Embedding<T>::~Embedding() {
     cudaFree(trec_);
     cudaFree(tstart_);
     cudaFree(acc_);
+    cudaFree(sorder_);
     if (h_pin_) cudaFreeHost(h_pin_);
     cudaFree(dgeom_);
     cudaFree(gstatus_);
@@ -486,7 +487,7 @@ int Embedding<T>::repulsion() {
     const size_t gridn = (D_ == 2) ? (size_t) M * M : (size_t) M;
     const int mode = (gp_.df == 1.0) ? KERNEL_DF1 : KERNEL_VARDF;
     FITSNE_CK(cudaMemsetAsync(grid_in_, 0, sizeof(Cell4<T>) * gridn, st_));
-    FITSNE_CK(launch_spread<T>(Y_[cur_], N_, D_, geom_, grid_in_, st_));
+    FITSNE_CK(launch_spread<T>(Y_[cur_], N_, D_, geom_, grid_in_, st_, data_order_ ? sorder_ : nullptr));
     if (timing_) FITSNE_CK(cudaEventRecord(evs_[tb_][2], st_));
     if (D_ == 2)
         FITSNE_CK(conv2d_launch<T>(grid_in_, grid_out_, M, plan_, tw_[L_], work_a_, work_b_, kspec_, geom_.hk,
@@ -544,25 +545,33 @@ int Embedding<T>::perm_to_host(std::vector<uint32_t> &out) {
     return 0;
 }
 
-// Renumbers the points along a Morton curve of the current embedding (reorder.cuh).
+// Buffers of the renumbering, allocated with the first one.
+template <typename T>
+int Embedding<T>::renumber_alloc() {
+    if (perm_) return 0;
+    FITSNE_CK(cudaMalloc(&perm_, sizeof(uint32_t) * N_));
+    FITSNE_CK(cudaMalloc(&iperm_, sizeof(uint32_t) * N_));
+    FITSNE_CK(cudaMalloc(&rkeys_, sizeof(uint32_t) * N_));
+    FITSNE_CK(cudaMalloc(&rids_, sizeof(uint32_t) * N_));
+    FITSNE_CK(cudaMalloc(&rkeys2_, sizeof(uint32_t) * N_));
+    FITSNE_CK(cudaMalloc(&rids2_, sizeof(uint32_t) * N_));
+    FITSNE_CK(cudaMalloc(&rlen_, sizeof(uint32_t) * (N_ + 1)));
+    FITSNE_CK(cudaMalloc(&row2_, sizeof(uint32_t) * (N_ + 1)));
+    FITSNE_CK(cudaMalloc(&col2_, sizeof(uint32_t) * (nnz_ ? nnz_ : 1)));
+    FITSNE_CK(cudaMalloc(&val2_, sizeof(T) * (nnz_ ? nnz_ : 1)));
+    const size_t scr = std::max(radix_sort_scratch_bytes(N_), scan_scratch_bytes((size_t) N_ + 1));
+    FITSNE_CK(cudaMalloc(&rscratch_, scr));
+    FITSNE_CK(launch_iota(perm_, N_, st_));
+    return 0;
+}
+
+// Renumbers the points along a Morton curve of the current embedding (reorder.cuh).  Points
+// numbered in the data's locality order keep it (the attraction's neighbour lists want it);
+// only the spread walks them in the Morton order then, so that a warp's points share boxes.
 template <typename T>
 int Embedding<T>::reorder() {
     const int W = y_width<T>(D_);
-    if (!perm_) {
-        FITSNE_CK(cudaMalloc(&perm_, sizeof(uint32_t) * N_));
-        FITSNE_CK(cudaMalloc(&iperm_, sizeof(uint32_t) * N_));
-        FITSNE_CK(cudaMalloc(&rkeys_, sizeof(uint32_t) * N_));
-        FITSNE_CK(cudaMalloc(&rids_, sizeof(uint32_t) * N_));
-        FITSNE_CK(cudaMalloc(&rkeys2_, sizeof(uint32_t) * N_));
-        FITSNE_CK(cudaMalloc(&rids2_, sizeof(uint32_t) * N_));
-        FITSNE_CK(cudaMalloc(&rlen_, sizeof(uint32_t) * (N_ + 1)));
-        FITSNE_CK(cudaMalloc(&row2_, sizeof(uint32_t) * (N_ + 1)));
-        FITSNE_CK(cudaMalloc(&col2_, sizeof(uint32_t) * (nnz_ ? nnz_ : 1)));
-        FITSNE_CK(cudaMalloc(&val2_, sizeof(T) * (nnz_ ? nnz_ : 1)));
-        const size_t scr = std::max(radix_sort_scratch_bytes(N_), scan_scratch_bytes((size_t) N_ + 1));
-        FITSNE_CK(cudaMalloc(&rscratch_, scr));
-        FITSNE_CK(launch_iota(perm_, N_, st_));
-    }
+    if (int ra = renumber_alloc()) return ra;
     // current bounds (also applies any pending mean shift)
     FITSNE_CK(launch_center_minmax<T>(Y_[cur_], N_, D_, mean_pending_ ? 1 : 0, excl_, red_, st_));
     mean_pending_ = false;
@@ -575,7 +584,36 @@ int Embedding<T>::reorder() {
     }
     FITSNE_CK(launch_morton_keys<T>(Y_[cur_], N_, D_, W, lo, hi, rkeys_, rids_, st_));
     FITSNE_CK(radix_sort_pairs(rkeys_, rids_, rkeys2_, rids2_, (size_t) N_, 32, rscratch_, st_));
-    const uint32_t *order = rids_;
+    if (data_order_) {
+        FITSNE_CK(cudaMemcpyAsync(sorder_, rids_, sizeof(uint32_t) * N_, cudaMemcpyDeviceToDevice, st_));
+        return 0;
+    }
+    return renumber(rids_);
+}
+
+// Numbers the points in the given order of the data space (data_locality_order): the
+// neighbour lists of consecutive rows overlap from the first iteration on, which the Morton
+// order of an embedding still taking shape does not give (N = 1M: the attraction 0.67 ms in
+// both phases, against 0.98 ms while the embedding is compact and 0.70 – 0.86 ms after, in the
+// Morton order).  The points keep this numbering; the spread walks them in the Morton order of
+// the embedding, refreshed at the iterations of the renumbering schedule.
+template <typename T>
+int Embedding<T>::set_order(const uint32_t *order) {
+    if (int ra = renumber_alloc()) return ra;
+    if (!sorder_) FITSNE_CK(cudaMalloc(&sorder_, sizeof(uint32_t) * N_));
+    FITSNE_CK(launch_iota(sorder_, N_, st_));
+    FITSNE_CK(cudaMemcpyAsync(rids_, order, sizeof(uint32_t) * N_, cudaMemcpyDeviceToDevice, st_));
+    if (int rn = renumber(rids_)) return rn;
+    data_order_ = true;
+    return 0;
+}
+
+// Internal point k becomes the current internal point order[k] (a permutation on the device):
+// point arrays, the CSR rows (in the new order) and columns (renamed), the tiles, and the map
+// to the caller's indices.
+template <typename T>
+int Embedding<T>::renumber(const uint32_t *order) {
+    const int W = y_width<T>(D_);
     FITSNE_CK(launch_invert(order, rkeys2_, N_, st_));  // rkeys2_ = inverse of order
     // point arrays
     FITSNE_CK(launch_gather_rows<T>(Y_[cur_], Y_[1 - cur_], order, N_, W, st_));
@@ -949,7 +987,8 @@ int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_f
                                   L_cap_, dgeom_, gstatus_, st_));
         FITSNE_CK(twiddles_dev<T>(cg, tw_dev_, st_));
         FITSNE_CK(cudaMemsetAsync(grid_in_, 0, sizeof(Cell4<T>) * gridn, st_));
-        FITSNE_CK(launch_spread_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_in_, st_));
+        FITSNE_CK(launch_spread_dev<T>(Y_[c], N_, D_, gp_.nterms, dgeom_, grid_in_, st_,
+                                       data_order_ ? sorder_ : nullptr));
         if (D_ == 2)
             FITSNE_CK(conv2d_launch_dev<T>(grid_in_, grid_out_, M_cap_, L_cap_, cg, tw_dev_, work_a_, work_b_, kspec_,
                                            gp_.df, mode, st_, fft_thr_));

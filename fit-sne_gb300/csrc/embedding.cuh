@@ -114,6 +114,10 @@ class Embedding {
                (it == 50 || it == 150 || it == 300 || it == 600 || (!reordered_ && it == it0 && it0 > 50));
     }
     int reorder_now() { return reorder(); }
+    // Numbers the points in a given order instead (order[k] = caller index of internal point
+    // k, on the device); the points keep it, and the renumbering schedule then only orders the
+    // spread's walk.
+    int set_order(const uint32_t *order);
     // Phase of the run for the attraction's launch shape: 0 while the embedding is compact
     // (early exaggeration and the first 50 iterations after it), 1 once it has expanded.  The
     // shapes rank differently in the two (N = 1M: 8 x 4 rows/edges 0.95 ms against 1.18 ms for
@@ -228,10 +232,16 @@ class Embedding {
     int gchunk_cur0_ = 0;
 
     // locality renumbering (reorder.cuh): perm_[k] = caller index of internal point k
+    int renumber_alloc();
+    int renumber(const uint32_t *order);
     int reorder();
     int perm_to_host(std::vector<uint32_t> &out);
     bool reorder_enabled_ = true;
     bool reordered_ = false;
+    // numbered in the data's locality order (set_order): the renumbering schedule then only
+    // refreshes sorder_, the Morton order in which the spread walks the points
+    bool data_order_ = false;
+    uint32_t *sorder_ = nullptr;
     int excl_ = 0;  // internal index of the caller's point 0 (min/max rule of the reference)
     uint32_t *perm_ = nullptr, *iperm_ = nullptr, *rkeys_ = nullptr, *rids_ = nullptr, *rkeys2_ = nullptr,
              *rids2_ = nullptr, *rlen_ = nullptr, *row2_ = nullptr, *col2_ = nullptr;

@@ -426,9 +426,12 @@ struct SpreadWarpTable {
 };
 constexpr int kSpreadWarps = kBlock / 32;
 
+// order (may be null): slot k of the walk takes point order[k] (a 2-D locality order of the
+// points when they are numbered by another one), so that a warp's points share boxes.
 template <int D>
 FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<float> &b,
-                               Cell4<float> *__restrict__ grid, int blk, int nblk) {
+                               Cell4<float> *__restrict__ grid, int blk, int nblk,
+                               const uint32_t *__restrict__ order = nullptr) {
     SpreadWarpTable *wb = nullptr;
     if constexpr (D == 2) {
         __shared__ SpreadWarpTable tables[kSpreadWarps];
@@ -456,7 +459,7 @@ FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<fl
         }
         if (valid) {
             df32 c[D];
-            YL<float, D>::load(Y, i, c);
+            YL<float, D>::load(Y, order ? (int) order[i] : i, c);
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 box_coord(c[d], b, bx[d], t[d]);
@@ -551,9 +554,10 @@ FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<fl
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_spread_runs(const float *__restrict__ Y, int N, BoxP<float> b,
                                                         Cell4<float> *__restrict__ grid,
-                                                        const DevGeom *__restrict__ dg) {
+                                                        const DevGeom *__restrict__ dg,
+                                                        const uint32_t *__restrict__ order) {
     if (dg) b = make_box(dg->g, (float *) nullptr);
-    spread_runs_body<D>(Y, N, b, grid, blockIdx.x, gridDim.x);
+    spread_runs_body<D>(Y, N, b, grid, blockIdx.x, gridDim.x, order);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1323,14 +1327,14 @@ cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, int excl, R
 
 template <typename T>
 cudaError_t spread_impl(const T *Y, int N, int D, int nterms, const BoxP<T> &b, Cell4<T> *grid, const DevGeom *dg,
-                        cudaStream_t st) {
+                        cudaStream_t st, const uint32_t *order = nullptr) {
     const int g = grid_for(N, kBlock, 1 << 20);
     if constexpr (sizeof(T) == 4) {
         if (nterms == 3) {
             if (D == 2)
-                k_spread_runs<2><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
+                k_spread_runs<2><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg, order);
             else
-                k_spread_runs<1><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg);
+                k_spread_runs<1><<<g, kBlock, 0, st>>>(Y, N, b, grid, dg, order);
             return cudaGetLastError();
         }
     }
@@ -1349,16 +1353,17 @@ cudaError_t spread_impl(const T *Y, int N, int D, int nterms, const BoxP<T> &b, 
 }
 
 template <typename T>
-cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &gg, Cell4<T> *grid, cudaStream_t st) {
-    return spread_impl<T>(Y, N, D, gg.nterms, make_box(gg, (T *) nullptr), grid, nullptr, st);
+cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &gg, Cell4<T> *grid, cudaStream_t st,
+                          const uint32_t *order) {
+    return spread_impl<T>(Y, N, D, gg.nterms, make_box(gg, (T *) nullptr), grid, nullptr, st, order);
 }
 
 template <typename T>
 cudaError_t launch_spread_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, Cell4<T> *grid,
-                              cudaStream_t st) {
+                              cudaStream_t st, const uint32_t *order) {
     BoxP<T> b{};
     b.nterms = nterms;
-    return spread_impl<T>(Y, N, D, nterms, b, grid, dg, st);
+    return spread_impl<T>(Y, N, D, nterms, b, grid, dg, st, order);
 }
 
 template <typename T>
@@ -1749,13 +1754,14 @@ int batch_attr_blocks_per_sm() {
 
 #define FITSNE_INST(T)                                                                                           \
     template cudaError_t launch_center_minmax<T>(T *, int, int, int, int, RedScratch, cudaStream_t);                \
-    template cudaError_t launch_spread<T>(const T *, int, int, const GridGeom &, Cell4<T> *, cudaStream_t);     \
+    template cudaError_t launch_spread<T>(const T *, int, int, const GridGeom &, Cell4<T> *, cudaStream_t,      \
+                                          const uint32_t *);                                                    \
     template cudaError_t launch_gather<T>(const T *, int, int, const GridGeom &, const Cell4<T> *, int, T *,     \
                                           RedScratch, cudaStream_t, float *);                                   \
     template cudaError_t launch_gather_dev<T>(const T *, int, int, int, const DevGeom *, const Cell4<T> *, int,  \
                                               T *, RedScratch, cudaStream_t, float *);                          \
     template cudaError_t launch_spread_dev<T>(const T *, int, int, int, const DevGeom *, Cell4<T> *,            \
-                                              cudaStream_t);                                                    \
+                                              cudaStream_t, const uint32_t *);                                  \
     template cudaError_t launch_attr_update<T>(const uint32_t *, const uint32_t *, const T *, const T *, T *,    \
                                                T *, T *, T *, const T *, int, int, const UpdateParams &,         \
                                                RedScratch, cudaStream_t, int, const float *);                   \

@@ -145,8 +145,11 @@ struct UpdateParams {
 // caller's point 0 after any internal renumbering).
 template <typename T>
 cudaError_t launch_center_minmax(T *Y, int N, int D, int apply_mean, int excl, RedScratch r, cudaStream_t st);
+// order (may be null): the FP32 nterms-3 spread walks the points as order[0], order[1], ...
+// (a 2-D locality order, so that a warp's points share boxes); the other forms ignore it
 template <typename T>
-cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &g, Cell4<T> *grid, cudaStream_t st);
+cudaError_t launch_spread(const T *Y, int N, int D, const GridGeom &g, Cell4<T> *grid, cudaStream_t st,
+                          const uint32_t *order = nullptr);
 // yh (may be null): FP32 form only, receives the high words of the positions (D floats per point)
 template <typename T>
 cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &g, const Cell4<T> *pot, int mode, T *rep,
@@ -154,7 +157,7 @@ cudaError_t launch_gather(const T *Y, int N, int D, const GridGeom &g, const Cel
 // As launch_spread / launch_gather with the geometry read from device memory.
 template <typename T>
 cudaError_t launch_spread_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, Cell4<T> *grid,
-                              cudaStream_t st);
+                              cudaStream_t st, const uint32_t *order = nullptr);
 template <typename T>
 cudaError_t launch_gather_dev(const T *Y, int N, int D, int nterms, const DevGeom *dg, const Cell4<T> *pot, int mode,
                               T *rep, RedScratch r, cudaStream_t st, float *yh = nullptr);

@@ -897,6 +897,11 @@ int locality_order(const double *Xd, int N, int D, uint32_t *perm, cudaStream_t 
 
 }  // namespace
 
+int data_locality_order(const double *Xd, int N, int D, uint32_t *order, cudaStream_t st, std::string &err) {
+    static_assert(kDataOrderMaxD == KD, "the pivot kernels read KD coordinates");
+    return locality_order(Xd, N, D, order, st, err);
+}
+
 int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, float *cand_d, uint32_t *cand_i,
                       cudaStream_t st, KnnTcStats *stats, std::string &err) {
     const int Npad = (N + BM - 1) / BM * BM;

@@ -24,6 +24,14 @@ struct KnnTcStats {
     double insert_iters_per_tile = 0, cycles_per_insert_iter = 0;  // epilogue warp level
 };
 
+// The locality order of the data that the tensor-core kNN also sorts its rows by: the points in
+// the cells of ~N/1024 pivots (evenly spaced rows of X; each point in the cell of its nearest),
+// the cells grouped by the nearest of 32 super-pivots.  order[r] = the point at row r.  Rows
+// close in this order are close in the data space, so their neighbour lists overlap.  It looks
+// at the first kDataOrderMaxD coordinates, which is all of them where it is used.
+constexpr int kDataOrderMaxD = 64;
+int data_locality_order(const double *Xd, int N, int D, uint32_t *order, cudaStream_t st, std::string &err);
+
 // True when the device is a Blackwell (cc 10.x) part, the driver exposes the tensor-map
 // encoder, D <= 62 (two spare columns of the 64-wide operand rows) and C <= kMaxTcCandidates.
 bool knn_tc_supported(int D, int C);

@@ -17,6 +17,7 @@
 #include "capi_internal.h"
 #include "embedding.cuh"
 #include "knn.cuh"
+#include "knn_tc.cuh"
 #include "session.cuh"
 
 namespace fitsne {
@@ -33,6 +34,12 @@ struct Stream {
     ~Stream() {
         if (s) cudaStreamDestroy(s);
     }
+};
+
+// the data's locality order on the device (build_P), freed with its scope
+struct DevOrder {
+    uint32_t *p = nullptr;
+    ~DevOrder() { cudaFree(p); }
 };
 
 // Gaussian random number of TSNE::randn (src/tsne.cpp:1880-1890), drawn from libc rand()
@@ -89,14 +96,37 @@ int save_p_files(int N, const std::vector<uint32_t> &row, const std::vector<uint
     return 0;
 }
 
+// Whether the embedding of N points of dimension D is numbered in the data's locality order
+// (data_locality_order; FITSNE_DATA_ORDER=0 leaves it to the Morton renumbering of the
+// embedding): embeddings large enough to be renumbered, data the order describes.
+bool data_order_wanted(int N, int D) {
+    const char *e = std::getenv("FITSNE_DATA_ORDER");
+    if (e && std::atoi(e) == 0) return false;
+    return N >= kReorderMinN && D <= kDataOrderMaxD;
+}
+
 // Similarity stage of TSNE::run (src/tsne.cpp:153-330): centre and scale X, exact kNN,
-// calibration, symmetrisation, normalisation; P stays on the device.
+// calibration, symmetrisation, normalisation; P stays on the device.  With order non-null and
+// data_order_wanted, *order receives the data's locality order (device memory, the caller frees
+// it); otherwise it is left null.
 int build_P(const double *X, int N, int D, double perplexity, int K, double sigma, int list_len, const double *list,
-            DevCSR *P, cudaStream_t st, bool vb, bool annoy_requested) {
+            DevCSR *P, cudaStream_t st, bool vb, bool annoy_requested, uint32_t **order = nullptr) {
     std::string err;
     const bool normalize = perplexity > 0 || list_len > 0;
     double *Xd = nullptr;
     if (prepare_X(X, N, D, normalize, &Xd, st, err)) return set_error(FITSNE_E_CUDA, err);
+    if (order) {
+        *order = nullptr;
+        if (data_order_wanted(N, D)) {
+            cudaError_t e = cudaMalloc(order, sizeof(uint32_t) * (size_t) N);
+            if (e != cudaSuccess || data_locality_order(Xd, N, D, *order, st, err)) {
+                cudaFree(*order);
+                *order = nullptr;
+                cudaFree(Xd);
+                return set_error(FITSNE_E_CUDA, e != cudaSuccess ? std::string(cudaGetErrorString(e)) : err);
+            }
+        }
+    }
     int K_use;
     double sigma_use;
     if (perplexity < 0) {
@@ -142,10 +172,11 @@ int build_P(const double *X, int N, int D, double perplexity, int K, double sigm
 
 template <typename T>
 int optimise(const DevCSR &P, double *Y, int N, int no_dims, const GridParams &gp, const Schedule &s, double *costs,
-             cudaStream_t st, bool vb) {
+             cudaStream_t st, bool vb, const uint32_t *order) {
     const auto t0 = std::chrono::steady_clock::now();
     Embedding<T> emb;
     int rc = emb.init_device(N, no_dims, P.row, P.col, P.val, P.nnz, Y, gp, st);
+    if (!rc && order) rc = emb.set_order(order);
     const auto t1 = std::chrono::steady_clock::now();
     if (!rc) rc = emb.run_schedule(s, 0, s.max_iter, costs, vb);
     const auto t2 = std::chrono::steady_clock::now();
@@ -306,6 +337,7 @@ int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexit
     Stream st;
     std::string err;
     DevCSR P;
+    DevOrder order;
     if (load_affinities == 1) {
         if (vb) std::printf("Loading approximate input similarities from files...\n");
         std::vector<uint32_t> row, col;
@@ -316,7 +348,7 @@ int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexit
             return set_error(FITSNE_E_CUDA, err);
     } else {
         rc = build_P(X, N, D, perplexity, K, sigma, perplexity_list_length, perplexity_list, &P, st.s, vb,
-                     knn_algo == 1);
+                     knn_algo == 1, &order.p);
         if (rc) return rc;
     }
     if (load_affinities == 2) {
@@ -374,9 +406,9 @@ int fitsne_run(double *X, int N, int D, double *Y, int no_dims, double perplexit
         costs = costs_local.data();
     }
     if (precision_bits() == 64)
-        rc = optimise<double>(P, Y, N, no_dims, gp, s, costs, st.s, vb);
+        rc = optimise<double>(P, Y, N, no_dims, gp, s, costs, st.s, vb, order.p);
     else
-        rc = optimise<float>(P, Y, N, no_dims, gp, s, costs, st.s, vb);
+        rc = optimise<float>(P, Y, N, no_dims, gp, s, costs, st.s, vb, order.p);
     free_csr(P);
     return rc;
 }
@@ -404,7 +436,9 @@ int fitsne_session_create_from_data(fitsne_session **out, const double *X, int N
     if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
         return set_error(FITSNE_E_CUDA, "cudaStreamCreate failed");
     DevCSR P;
-    rc = build_P(X, N, D, perplexity, K, sigma, perplexity_list_length, perplexity_list, &P, st, false, false);
+    DevOrder order;
+    rc = build_P(X, N, D, perplexity, K, sigma, perplexity_list_length, perplexity_list, &P, st, false, false,
+                 &order.p);
     if (rc) {
         cudaStreamDestroy(st);
         return rc;
@@ -420,10 +454,12 @@ int fitsne_session_create_from_data(fitsne_session **out, const double *X, int N
         auto *p = new SessionT<double>;
         s->impl.reset(p);
         rc = p->emb.init_device(N, no_dims, P.row, P.col, P.val, P.nnz, Y0, gp, st);
+        if (!rc && order.p) rc = p->emb.set_order(order.p);
     } else {
         auto *p = new SessionT<float>;
         s->impl.reset(p);
         rc = p->emb.init_device(N, no_dims, P.row, P.col, P.val, P.nnz, Y0, gp, st);
+        if (!rc && order.p) rc = p->emb.set_order(order.p);
     }
     free_csr(P);
     s->impl->st = st;

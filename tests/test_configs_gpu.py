@@ -167,6 +167,29 @@ def test_c2_gradient_every_50_iterations_against_the_oracle(gpu_lib, orc, c2):
     assert worst > 0.0
 
 
+def test_c2_session_from_data_in_the_data_order_against_the_oracle(gpu_lib, orc, c2):
+    """The same configuration through Session.from_data: the library builds P itself and, the
+    data being 50-D and the embedding large enough to be renumbered, numbers the points in the
+    data's locality order from the start.  Every 150 iterations its gradient, returned in the
+    caller's order, matches the restated reference gradient on the same Y and on P built in the
+    caller's order."""
+    X, (row, col, val) = c2
+    N = len(X)
+    Y0 = np.random.default_rng(1).standard_normal((N, 2)) * 1e-4
+    s = gpu_lib.Session.from_data(X, Y0, perplexity=30.0, precision=32)
+    try:
+        assert s.nnz == len(col)
+        for it in range(0, 750, 150):
+            s.run(it, it + 150, max_iter=750, learning_rate=N / 12.0)
+            Y = s.get_y()
+            d32, z32 = s.gradient()
+            dref, zref = orc.fft_gradient(row, col, val, Y, 3, 1.0, 50, NT, 1.0)
+            assert rel_l2(d32, dref) <= 1e-4, (it + 150, rel_l2(d32, dref))
+            assert abs(z32 - zref) <= 1e-5 * zref, (it + 150, z32, zref)
+    finally:
+        s.close()
+
+
 def test_c2_knn_lists_match_the_restated_vptree(gpu_lib, orc, c2):
     """Neighbour lists of the 70,000-point data (K = 90) against the restated VP-tree search
     (src/tsne.cpp:1643-1726, vptree.h): the same index sets except within groups of equal
