@@ -809,7 +809,8 @@ int Embedding<T>::run_schedule(const Schedule &s, int it0, int it1, double *cost
 // step of this embedding's data (on scratch copies of the state) and the fastest is kept.
 // Choices are made per phase of the run (tune_phase: compact or expanded embedding) and shared
 // by embeddings of the same size class (type, dimension, log2 N, log2 nnz / N, renumbered or
-// not, phase) within the process.  An embedding that will be renumbered runs the default shape
+// not, phase, tiled form available or not, numbered in the data's order or not) within the
+// process.  An embedding that will be renumbered runs the default shape
 // until its first renumbering.  One-off gradients (measure false) take the cached choice or the
 // default.
 template <typename T>
@@ -830,7 +831,8 @@ int Embedding<T>::tune_attr(bool measure) {
     while ((1 << (lgN + 1)) <= N_) ++lgN;
     const size_t per = N_ ? nnz_ / (size_t) N_ : 0;
     while (((size_t) 1 << (lgK + 1)) <= per) ++lgK;
-    const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0, tune_phase_, tiles_ok_ ? 1 : 0};
+    const std::vector<int> key = {(int) sizeof(T), D_, lgN, lgK, reordered_ ? 1 : 0, tune_phase_,
+                                  tiles_ok_ ? 1 : 0, data_order_ ? 1 : 0};
     attr_phase_ = tune_phase_;
     const char *fixed = std::getenv("FITSNE_ATTR_SHAPE");  // a fixed shape index: no tuning, no cache
     if (fixed && *fixed) {
