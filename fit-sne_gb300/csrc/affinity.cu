@@ -263,7 +263,7 @@ __global__ void k_row_src(const uint32_t *__restrict__ row, int N, uint32_t *__r
 }
 
 // per-row copy of (col, position) sorted by col (insertion sort; rows are short)
-// Rows longer than kWarpRow entries (the warp-per-row kernels below take the others).
+// Rows longer than kWarpRow entries (k_row_sorted_warp below sorts the others).
 constexpr int kWarpRow = 256;
 
 __global__ void k_row_sorted(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col, int N,
@@ -312,69 +312,14 @@ __global__ void k_count_in(const uint32_t *__restrict__ col, size_t nnz, uint32_
         atomicAdd(&indeg[col[e]], 1u);
 }
 
-// Output row r: incoming n < r (ascending), r's own entries in list order except those
-// mirrored earlier, incoming n > r that r does not list (ascending)  (tsne.cpp:1772-1811).
-// Only the rows with more than kWarpRow entries or incoming edges (the warp-per-row kernel
-// below takes the others).
-template <bool FILL>
-__global__ void k_sym_rows(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
-                           const double *__restrict__ val, const uint32_t *__restrict__ scol,
-                           const uint32_t *__restrict__ spos, const uint32_t *__restrict__ toff,
-                           const uint32_t *__restrict__ tedge, const uint32_t *__restrict__ src, int N,
-                           uint32_t *__restrict__ count, const uint32_t *__restrict__ srow,
-                           uint32_t *__restrict__ ocol, double *__restrict__ oval) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
-        if (row[r + 1] - row[r] <= (uint32_t) kWarpRow && toff[r + 1] - toff[r] <= (uint32_t) kWarpRow) continue;
-        uint32_t o = FILL ? srow[r] : 0u;
-        uint32_t c0 = 0;
-        const uint32_t ur = (uint32_t) r;
-        // first group: incoming n < r
-        for (uint32_t t = toff[r]; t < toff[r + 1]; ++t) {
-            const uint32_t e = tedge[t];
-            const uint32_t n = src[e];
-            if (n >= ur) break;
-            if (FILL) {
-                const uint32_t m = find_in_row(row, scol, spos, ur, n);
-                ocol[o] = n;
-                oval[o] = (m != 0xffffffffu) ? (val[e] + val[m]) / 2.0 : val[e] / 2.0;
-                ++o;
-            }
-            ++c0;
-        }
-        // middle: own entries
-        for (uint32_t e = row[r]; e < row[r + 1]; ++e) {
-            const uint32_t c = col[e];
-            const uint32_t m = find_in_row(row, scol, spos, c, ur);
-            if (m != 0xffffffffu && c < ur) continue;
-            if (FILL) {
-                ocol[o] = c;
-                oval[o] = (m != 0xffffffffu) ? (val[e] + val[m]) / 2.0 : val[e] / 2.0;
-                ++o;
-            }
-            ++c0;
-        }
-        // last group: incoming n > r not listed by r
-        for (uint32_t t = toff[r]; t < toff[r + 1]; ++t) {
-            const uint32_t e = tedge[t];
-            const uint32_t n = src[e];
-            if (n <= ur) continue;
-            if (find_in_row(row, scol, spos, ur, n) != 0xffffffffu) continue;
-            if (FILL) {
-                ocol[o] = n;
-                oval[o] = val[e] / 2.0;
-                ++o;
-            }
-            ++c0;
-        }
-        if (!FILL) count[r] = c0;
-    }
-}
-
 // ---------------------------------------------------------------------------------
-// Warp-per-row forms of k_row_sorted and k_sym_rows for rows of at most kWarpRow entries (the
-// kNN rows: K per row; longer rows keep the thread-per-row kernels above).  Same outputs,
-// entry for entry: the sort is by column (columns of a row are distinct), and each group of
-// an output row is compacted in its own order with warp ballots.
+// Warp per row.  k_row_sorted_warp sorts rows of at most kWarpRow entries (the kNN rows: K per
+// row; longer rows: k_row_sorted above, a thread each); the sort is by column (columns of a
+// row are distinct).  k_sym_rows_warp writes every output row (tsne.cpp:1772-1811): incoming
+// n < r (ascending), r's own entries in list order except those mirrored earlier, incoming
+// n > r that r does not list (ascending).  It streams a row's entries and incoming edges in
+// chunks of 32 and compacts each group in its own order with warp ballots, so a hub row (many
+// incoming edges) costs its warp (incoming / 32) rounds.
 
 __global__ void __launch_bounds__(128) k_row_sorted_warp(const uint32_t *__restrict__ row,
                                                          const uint32_t *__restrict__ col, int N,
@@ -416,8 +361,7 @@ __global__ void __launch_bounds__(128) k_row_sorted_warp(const uint32_t *__restr
     }
 }
 
-// One warp per output row; rows with more than kWarpRow entries or incoming edges are left to
-// k_sym_rows (long_rows set).
+// One warp per output row, every row (see above).
 template <bool FILL>
 __global__ void __launch_bounds__(128) k_sym_rows_warp(const uint32_t *__restrict__ row,
                                                        const uint32_t *__restrict__ col,
@@ -428,18 +372,13 @@ __global__ void __launch_bounds__(128) k_sym_rows_warp(const uint32_t *__restric
                                                        const uint32_t *__restrict__ tedge,
                                                        const uint32_t *__restrict__ src, int N,
                                                        uint32_t *__restrict__ count, const uint32_t *__restrict__ srow,
-                                                       uint32_t *__restrict__ ocol, double *__restrict__ oval,
-                                                       int *__restrict__ long_rows) {
+                                                       uint32_t *__restrict__ ocol, double *__restrict__ oval) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     for (int r = gw; r < N; r += nw) {
         const uint32_t ur = (uint32_t) r;
         const uint32_t r0 = row[r], r1 = row[r + 1], t0 = toff[r], t1 = toff[r + 1];
-        if (r1 - r0 > (uint32_t) kWarpRow || t1 - t0 > (uint32_t) kWarpRow) {
-            if (lane == 0) atomicOr(long_rows, 1);
-            continue;
-        }
         uint32_t o = FILL ? srow[r] : 0u;
         uint32_t c0 = 0;
         const uint32_t lanemask = (1u << lane) - 1u;
@@ -632,7 +571,7 @@ int calibrate_rows(const double *dist, int stride, int offset, double *P, int nr
 
 int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double perplexity, double sigma, int list_len,
                                const double *list_host, DevCSR *out, cudaStream_t st, std::string &err,
-                               int *knn_rescanned) {
+                               int *knn_rescanned, uint32_t *order_out, bool *order_written) {
     if (K < 1 || K + 1 > N) {
         err = "K + 1 must not exceed the number of points";
         return -3;
@@ -645,7 +584,7 @@ int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double per
     const char *kerr = nullptr;
     const bool tm = timing_requested();
     const double t0 = now_s();
-    int rc = knn_exact(Xd, N, D, K + 1, idx, dist, st, &ks, &kerr);
+    int rc = knn_exact(Xd, N, D, K + 1, idx, dist, st, &ks, &kerr, order_out, order_written);
     if (tm) print_knn_stats(K + 1, ks, now_s() - t0);
     if (rc) {
         err = kerr ? kerr : "kNN failed";
@@ -739,14 +678,7 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     ACK(exclusive_scan_u32(indeg, toff, (size_t) N, scratch, st));
     const int gw = std::min((N + 3) / 4, 8192);
     k_sym_rows_warp<false><<<gw, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, cnt, nullptr,
-                                               nullptr, nullptr, long_rows + 1);
-    ACK(cudaMemcpyAsync(hlong + 1, long_rows + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    ACK(cudaStreamSynchronize(st));
-    // rows with more than kWarpRow entries or incoming edges: a thread each
-    const bool thread_rows = hlong[0] || hlong[1];
-    if (thread_rows)
-        k_sym_rows<false><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
-                                                           cnt, nullptr, nullptr, nullptr);
+                                               nullptr, nullptr);
     DevCSR P;
     P.N = N;
     ACK(cudaMalloc(&P.row, sizeof(uint32_t) * (N + 1)));
@@ -758,10 +690,7 @@ int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::strin
     ACK(cudaMalloc(&P.col, sizeof(uint32_t) * (total ? total : 1)));
     ACK(cudaMalloc(&P.val, sizeof(double) * (total ? total : 1)));
     k_sym_rows_warp<true><<<gw, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N, nullptr,
-                                              P.row, P.col, P.val, long_rows + 1);
-    if (thread_rows)
-        k_sym_rows<true><<<(N + 127) / 128, 128, 0, st>>>(in.row, in.col, in.val, scol, spos, toff, tedge, src, N,
-                                                          nullptr, P.row, P.col, P.val);
+                                              P.row, P.col, P.val);
     ACK(cudaGetLastError());
     ACK(cudaStreamSynchronize(st));
     cudaFree(src);

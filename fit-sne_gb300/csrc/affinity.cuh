@@ -46,9 +46,12 @@ int calibrate_rows(const double *dist, int stride, int offset, double *P, int nr
                    std::string &err, std::vector<int> *iters = nullptr);
 
 // kNN + calibration into fixed-length rows (row n = n*K).  Xd on the device.
+// order_out / order_written (may be null): the kNN's locality order, when it used one
+// (knn_candidates_tc, knn_tc.cuh).
 int gaussian_perplexity_device(const double *Xd, int N, int D, int K, double perplexity, double sigma, int list_len,
                                const double *list_host, DevCSR *out, cudaStream_t st, std::string &err,
-                               int *knn_rescanned = nullptr);
+                               int *knn_rescanned = nullptr, uint32_t *order_out = nullptr,
+                               bool *order_written = nullptr);
 
 // (P + P^T)/2 in the reference's entry order.  in is left untouched.
 int symmetrize_device(const DevCSR &in, DevCSR *out, cudaStream_t st, std::string &err);

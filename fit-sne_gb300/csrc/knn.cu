@@ -361,7 +361,7 @@ void print_knn_stats(int K, const KnnStats &ks, double total_s) {
 }
 
 int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist, cudaStream_t st, KnnStats *stats,
-              const char **err) {
+              const char **err, uint32_t *order_out, bool *order_written) {
     static thread_local std::string msg;
     auto fail = [&](const char *what, cudaError_t e) {
         msg = std::string(what) + ": " + cudaGetErrorString(e);
@@ -426,7 +426,8 @@ int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist
         KCK(cudaMalloc(&cd, sizeof(float) * (size_t) N * C));
         KCK(cudaMalloc(&ci, sizeof(uint32_t) * (size_t) N * C));
         std::string terr;
-        if (knn_candidates_tc(Xd, N, D, C, maxnorm, cd, ci, st, stats ? &stats->tc : nullptr, terr) != 0) {
+        if (knn_candidates_tc(Xd, N, D, C, maxnorm, cd, ci, st, stats ? &stats->tc : nullptr, terr, order_out,
+                              order_written) != 0) {
             msg = terr;
             if (err) *err = msg.c_str();
             cudaFree(Xf);

@@ -36,7 +36,8 @@ void print_knn_stats(int K, const KnnStats &ks, double total_s);
 // Xd: N x D FP64 (device).  Writes idx[N*K] and dist[N*K] (device, FP64 non-squared,
 // ascending).  K includes the point itself (the reference asks for K + 1 neighbours).
 // Returns 0 or a negative error code; err receives a message.
+// order_out / order_written (may be null): see knn_candidates_tc (knn_tc.cuh).
 int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist, cudaStream_t st, KnnStats *stats,
-              const char **err);
+              const char **err, uint32_t *order_out = nullptr, bool *order_written = nullptr);
 
 }  // namespace fitsne

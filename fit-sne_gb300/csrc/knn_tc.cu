@@ -903,7 +903,8 @@ int data_locality_order(const double *Xd, int N, int D, uint32_t *order, cudaStr
 }
 
 int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, float *cand_d, uint32_t *cand_i,
-                      cudaStream_t st, KnnTcStats *stats, std::string &err) {
+                      cudaStream_t st, KnnTcStats *stats, std::string &err, uint32_t *order_out,
+                      bool *order_written) {
     const int Npad = (N + BM - 1) / BM * BM;
     const size_t plane = (size_t) Npad * KD;
     const int nQT = Npad / BM, nRT = Npad / BN;
@@ -936,6 +937,15 @@ int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, flo
         if (rc) {
             cleanup();
             return rc;
+        }
+        if (order_out) {
+            if ((e = cudaMemcpyAsync(order_out, perm, sizeof(uint32_t) * N, cudaMemcpyDeviceToDevice, st)) !=
+                cudaSuccess) {
+                err = std::string("knn order copy: ") + cudaGetErrorString(e);
+                cleanup();
+                return -10;
+            }
+            if (order_written) *order_written = true;
         }
     }
     const size_t nb = (size_t) (nQT + nRT + nSB) * (KD + 1);

@@ -58,8 +58,11 @@ bool knn_tc_supported(int D, int C);
 // Exactness: a skipped point would not have entered the list had its tile been computed (its
 // approximate d^2 is above the threshold then in force, and thresholds only fall), so the
 // lists are the ones the full scan keeps, up to the order of equal approximate distances.
+// order_out (may be null, device, N entries): receives the locality order when the search used
+// one, and *order_written is then set (data_locality_order gives the same order).
 int knn_candidates_tc(const double *Xd, int N, int D, int C, double maxnorm, float *cand_d, uint32_t *cand_i,
-                      cudaStream_t st, KnnTcStats *stats, std::string &err);
+                      cudaStream_t st, KnnTcStats *stats, std::string &err, uint32_t *order_out = nullptr,
+                      bool *order_written = nullptr);
 
 // 1: locality order before the candidate search (default), 0: the caller's order
 // (FITSNE_KNN_ORDER=input).

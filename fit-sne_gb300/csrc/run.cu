@@ -115,15 +115,16 @@ int build_P(const double *X, int N, int D, double perplexity, int K, double sigm
     const bool normalize = perplexity > 0 || list_len > 0;
     double *Xd = nullptr;
     if (prepare_X(X, N, D, normalize, &Xd, st, err)) return set_error(FITSNE_E_CUDA, err);
+    // the order (the kNN writes it when its search used it; otherwise computed here)
+    bool order_written = false;
     if (order) {
         *order = nullptr;
         if (data_order_wanted(N, D)) {
-            cudaError_t e = cudaMalloc(order, sizeof(uint32_t) * (size_t) N);
-            if (e != cudaSuccess || data_locality_order(Xd, N, D, *order, st, err)) {
-                cudaFree(*order);
+            const cudaError_t e = cudaMalloc(order, sizeof(uint32_t) * (size_t) N);
+            if (e != cudaSuccess) {
                 *order = nullptr;
                 cudaFree(Xd);
-                return set_error(FITSNE_E_CUDA, e != cudaSuccess ? std::string(cudaGetErrorString(e)) : err);
+                return set_error(FITSNE_E_CUDA, cudaGetErrorString(e));
             }
         }
     }
@@ -152,9 +153,16 @@ int build_P(const double *X, int N, int D, double perplexity, int K, double sigm
     }
     DevCSR P0;
     int rc = gaussian_perplexity_device(Xd, N, D, K_use, perplexity, sigma_use, perplexity == 0 ? list_len : 0, list,
-                                        &P0, st, err);
+                                        &P0, st, err, nullptr, order ? *order : nullptr, &order_written);
+    if (!rc && order && *order && !order_written) rc = data_locality_order(Xd, N, D, *order, st, err);
     cudaFree(Xd);
-    if (rc) return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
+    if (rc) {
+        if (order) {
+            cudaFree(*order);
+            *order = nullptr;
+        }
+        return set_error(rc == -3 ? FITSNE_E_ARG : FITSNE_E_CUDA, err);
+    }
     const auto t0 = std::chrono::steady_clock::now();
     rc = symmetrize_device(P0, P, st, err);
     free_csr(P0);
