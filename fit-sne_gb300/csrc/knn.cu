@@ -26,6 +26,11 @@ __device__ __forceinline__ bool pair_gt(float a, uint32_t ia, float b, uint32_t 
 __device__ __forceinline__ bool pair_gt(double a, uint32_t ia, double b, uint32_t ib) {
     return a > b || (a == b && ia > ib);
 }
+// non-negative doubles by their bit patterns (the same order; integer compares instead of the
+// FP64 pipe, whose warp instructions cost GB300 many cycles)
+__device__ __forceinline__ bool pair_gt(unsigned long long a, uint32_t ia, unsigned long long b, uint32_t ib) {
+    return a > b || (a == b && ia > ib);
+}
 
 // ascending bitonic sort of n (power of two) (key, index) pairs in shared memory by one warp
 template <typename KT>
@@ -193,6 +198,13 @@ __global__ void __launch_bounds__(kThreads) k_knn_cand(const float *__restrict__
 }
 
 // FP64 re-rank of the candidates of each query (one warp per query) + verification.
+//
+// The FP64 distances are the reference's (sequential sum of rounded squared differences, then
+// the square root).  GB300's FP64 pipe charges each warp instruction whatever the lanes
+// active, so the work goes by chunks of 32 candidates: a chunk whose candidates are all
+// farther (by their approximate squared distances) than the K-th one plus twice the error
+// bound of the approximation cannot hold one of the K nearest, and is not evaluated (its
+// entries sort last).  The sort compares the non-negative distances as integers.
 template <int CP>
 __global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ Xd, int N, int D, int K, int C,
                                                     const int *__restrict__ qlist, int nq,
@@ -209,10 +221,20 @@ __global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ X
     if (slot >= nq) return;
     const int q = qlist ? qlist[slot] : slot;
     const double *xq = Xd + (size_t) q * D;
+    // bound on |approximate - exact| squared distance of every candidate (all are at most the
+    // C-th approximate one): the verification's below
+    const double u = 5.9604644775390625e-08;  // 2^-24
+    const double xn = norms[q];
+    const double sC = (double) cand_d[(size_t) slot * C + C - 1];
+    const double eps = tc ? 1.5 * (D + 4) * u * sC + 3e-5 * xn * maxnorm + 4e-6 * (xn * xn + maxnorm * maxnorm) + 1e-30
+                          : 1.5 * ((D + 4) * u * sC + 4.0 * u * sqrt(sC) * (xn + maxnorm)) + 1e-30;
+    const double cut = (double) cand_d[(size_t) slot * C + (K < C ? K : C) - 1] + 2.0 * eps;
     for (int c = lane; c < CP; c += 32) {
         double e = DBL_MAX;
         uint32_t j = 0xffffffffu;
-        if (c < C) {
+        // the chunk is evaluated when one of its candidates may be among the K nearest
+        const bool may = c < C && (c < K || (double) cand_d[(size_t) slot * C + c] <= cut);
+        if (__any_sync(0xffffffffu, may) && c < C) {
             j = cand_i[(size_t) slot * C + c];
             if (j != 0xffffffffu) {
                 const double *xj = Xd + (size_t) j * D;
@@ -228,7 +250,7 @@ __global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ X
         ei[c] = j;
     }
     __syncwarp();
-    warp_bitonic<double>(ed, ei, CP);
+    warp_bitonic<unsigned long long>(reinterpret_cast<unsigned long long *>(ed), ei, CP);
     for (int k = lane; k < K; k += 32) {
         idx[(size_t) q * K + k] = ei[k];
         dist[(size_t) q * K + k] = ed[k];
@@ -236,14 +258,9 @@ __global__ void __launch_bounds__(128) k_knn_rerank(const double *__restrict__ X
     if (lane == 0) {
         int ok = 1;
         if (C < N) {
-            // every point outside the list has an FP32 squared distance >= the C-th one
-            const double sC = (double) cand_d[(size_t) slot * C + C - 1];
-            const double u = 5.9604644775390625e-08;  // 2^-24
-            const double nq = norms[q];
-            // FP32 direct differences (SIMT scan) or BF16 hi/lo tensor-core products (knn_tc.cuh)
-            const double eps =
-                tc ? 1.5 * (D + 4) * u * sC + 3e-5 * nq * maxnorm + 4e-6 * (nq * nq + maxnorm * maxnorm) + 1e-30
-                   : 1.5 * ((D + 4) * u * sC + 4.0 * u * sqrt(sC) * (nq + maxnorm)) + 1e-30;
+            // every point outside the list has an approximate squared distance >= the C-th
+            // one, sC; eps bounds the approximation: FP32 direct differences (SIMT scan) or
+            // BF16 hi/lo tensor-core products (knn_tc.cuh)
             const double sK = ed[K - 1] * ed[K - 1];
             ok = (sK < sC - eps) ? 1 : 0;
         }
