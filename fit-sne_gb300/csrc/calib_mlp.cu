@@ -106,11 +106,35 @@ __global__ void __launch_bounds__(H) k_mlp_grad(const float *__restrict__ params
     const unsigned full = 0xffffffffu;
     const int u = threadIdx.x;
     const Offs o = offs(K);
-#pragma unroll 8
-    for (int r = 0; r < H; ++r)
-        for (int c = u; c < K; c += H) W1[r * KP + c] = params[o.w1 + r * K + c];
-#pragma unroll 8
-    for (int r = 0; r < H; ++r) W2[r * kH2 + u] = params[o.w2 + r * H + u];
+    // the weights into shared memory with 16-byte loads (W1 and W2 start on 16-byte boundaries:
+    // offsets 0 and 64 K + 64 floats); a vector of W1 may run into the next row
+    {
+        const float4 *p1 = reinterpret_cast<const float4 *>(params + o.w1);
+#pragma unroll 4
+        for (int e = u; e < H * K / 4; e += H) {
+            const float4 w = __ldg(p1 + e);
+            const float wv[4] = {w.x, w.y, w.z, w.w};
+            int r = (4 * e) / K, c = 4 * e - r * K;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                W1[r * KP + c] = wv[k];
+                if (++c == K) {
+                    c = 0;
+                    ++r;
+                }
+            }
+        }
+        const float4 *p2 = reinterpret_cast<const float4 *>(params + o.w2);
+#pragma unroll 4
+        for (int e = u; e < H * H / 4; e += H) {
+            const float4 w = __ldg(p2 + e);
+            const int r = (4 * e) / H, c = (4 * e) % H;
+            W2[r * kH2 + c] = w.x;
+            W2[r * kH2 + c + 1] = w.y;
+            W2[r * kH2 + c + 2] = w.z;
+            W2[r * kH2 + c + 3] = w.w;
+        }
+    }
     const float b1 = params[o.b1 + u], b2 = params[o.b2 + u], w3 = params[o.w3 + u], b3 = params[o.b3];
     const unsigned stp = step ? *step : 0u;
     // the block's samples and targets in one round of loads; samples past the batch are zero
