@@ -1,4 +1,5 @@
 // Exact kNN: FP32 candidate scan + FP64 re-rank with verification (see knn.cuh).
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -435,7 +436,9 @@ int knn_exact(const double *Xd, int N, int D, int K, uint32_t *idx, double *dist
     auto secs = [&clk0]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - clk0).count(); };
     const char *mode = std::getenv("FITSNE_KNN");
     const bool force_simt = mode && std::string(mode) == "simt";
-    const int Ctc = K + kTcSlack < N ? K + kTcSlack : N;
+    int slack = kTcSlack;  // FITSNE_KNN_SLACK overrides it
+    if (const char *es = std::getenv("FITSNE_KNN_SLACK")) slack = std::max(0, std::atoi(es));
+    const int Ctc = K + slack < N ? K + slack : N;
     const bool use_tc = !force_simt && N >= 256 && knn_tc_supported(D, Ctc);
     if (use_tc) {
         C = Ctc;
