@@ -64,7 +64,10 @@ Embedding<T>::~Embedding() {
     cudaFree(tw_dev_);
     cudaFree(snap_);
     cudaFree(snap_mean_);
-    if (gexec_) cudaGraphExecDestroy(gexec_);
+    for (auto &a : gslots_)
+        for (auto &b : a)
+            for (auto &s : b)
+                if (s.exec) cudaGraphExecDestroy(s.exec);
     for (auto &b : evs_)
         for (auto &e : b)
             if (e) cudaEventDestroy(e);
@@ -970,20 +973,12 @@ int Embedding<T>::plan_capacity(int grow) {
 }
 
 template <typename T>
-int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_first) {
-    const int W = y_width<T>(D_);
-    const size_t ny = (size_t) N_ * W, nd = (size_t) N_ * D_;
-    int c = cur_;
-    FITSNE_CK(cudaMemcpyAsync(snap_, Y_[c], sizeof(T) * ny, cudaMemcpyDeviceToDevice, st_));
-    FITSNE_CK(cudaMemcpyAsync(snap_ + ny, uY_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
-    FITSNE_CK(cudaMemcpyAsync(snap_ + ny + nd, gains_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
-    FITSNE_CK(cudaMemcpyAsync(snap_mean_, red_.mean, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st_));
-    FITSNE_CK(cudaMemsetAsync(gstatus_, 0, sizeof(int), st_));
+int Embedding<T>::record_iters(const UpdateParams &p, int n, int c, bool apply_mean_first) {
     const int mode = (gp_.df == 1.0) ? KERNEL_DF1 : KERNEL_VARDF;
     const ConvGeom *cg =
         reinterpret_cast<const ConvGeom *>(reinterpret_cast<const char *>(dgeom_) + offsetof(DevGeom, conv));
     const size_t gridn = (D_ == 2) ? (size_t) M_cap_ * M_cap_ : (size_t) M_cap_;
-    for (int k = 0; k < len; ++k) {
+    for (int k = 0; k < n; ++k) {
         FITSNE_CK(launch_center_minmax<T>(Y_[c], N_, D_, (k > 0 || apply_mean_first) ? 1 : 0, excl_, red_, st_));
         FITSNE_CK(launch_geometry(red_, D_, gp_.nterms, gp_.intervals_per_integer, gp_.min_num_intervals, nb_cap_,
                                   L_cap_, dgeom_, gstatus_, st_));
@@ -1001,12 +996,49 @@ int Embedding<T>::record_chunk(const UpdateParams &p, int len, bool apply_mean_f
                             attr_shape_ < 0 ? (sizeof(T) == 4 ? 10 : 3) : attr_shape_));
         c = 1 - c;
     }
-    FITSNE_CK(cudaMemcpyAsync(h_gstat_, gstatus_, sizeof(int), cudaMemcpyDeviceToHost, st_));
-    FITSNE_CK(cudaMemcpyAsync(h_gstat_ + 1,
-                              reinterpret_cast<const char *>(dgeom_) + offsetof(DevGeom, g) + offsetof(GridGeom, nb),
-                              sizeof(int), cudaMemcpyDeviceToHost, st_));
-    gchunk_len_ = len;
-    gchunk_cur0_ = cur_;
+    return 0;
+}
+
+template <typename T>
+int Embedding<T>::launch_iters(const UpdateParams &p, int n, int c, bool apply_mean_first) {
+    GraphSlot &s = gslots_[n - 1][c][apply_mean_first ? 1 : 0];
+    const std::vector<unsigned long long> key = iters_key(p, n, c, apply_mean_first);
+    if (!s.exec || key != s.key) {
+        cudaGraph_t graph = nullptr;
+        FITSNE_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeRelaxed));
+        int rc = record_iters(p, n, c, apply_mean_first);
+        cudaError_t ce = cudaStreamEndCapture(st_, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        // same topology (a new capacity, new buffers after a renumbering, new schedule
+        // parameters): update the instantiated graph in place, else instantiate anew
+        bool updated = false;
+        if (ce == cudaSuccess && s.exec) {
+            cudaGraphExecUpdateResultInfo info;
+            updated = cudaGraphExecUpdate(s.exec, graph, &info) == cudaSuccess;
+            if (!updated) cudaGetLastError();  // clear the failed update
+        }
+        if (ce == cudaSuccess && !updated) {
+            if (s.exec) {
+                cudaGraphExecDestroy(s.exec);
+                s.exec = nullptr;
+            }
+            ce = cudaGraphInstantiate(&s.exec, graph, 0);
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) {
+            if (s.exec) cudaGraphExecDestroy(s.exec);
+            s.exec = nullptr;
+            s.key.clear();
+            return fail("iterations graph", ce);
+        }
+        s.key = key;
+        ++captures_;
+        if (updated) ++updates_;
+    }
+    FITSNE_CK(cudaGraphLaunch(s.exec, st_));
     return 0;
 }
 
@@ -1040,57 +1072,45 @@ template <typename T>
 int Embedding<T>::launch_chunk(const UpdateParams &p, int len, int grow) {
     int rc = plan_capacity(grow);
     if (rc) return rc;
-    const bool am = mean_pending_;
-    const std::vector<unsigned long long> key = chunk_key(p, len);
-    if (!gexec_ || key != gkey_) {
-        cudaGraph_t graph = nullptr;
-        FITSNE_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeRelaxed));
-        rc = record_chunk(p, len, am);
-        cudaError_t ce = cudaStreamEndCapture(st_, &graph);
-        if (rc) {
-            if (graph) cudaGraphDestroy(graph);
-            return rc;
-        }
-        // same topology (a new capacity, new buffers after a renumbering, new schedule
-        // parameters): update the instantiated graph in place, else instantiate anew
-        bool updated = false;
-        if (ce == cudaSuccess && gexec_ && gexec_len_ == len) {
-            cudaGraphExecUpdateResultInfo info;
-            updated = cudaGraphExecUpdate(gexec_, graph, &info) == cudaSuccess;
-            if (!updated) cudaGetLastError();  // clear the failed update
-        }
-        if (ce == cudaSuccess && !updated) {
-            if (gexec_) {
-                cudaGraphExecDestroy(gexec_);
-                gexec_ = nullptr;
-            }
-            ce = cudaGraphInstantiate(&gexec_, graph, 0);
-        }
-        if (graph) cudaGraphDestroy(graph);
-        if (ce != cudaSuccess) return fail("chunk graph", ce);
-        gkey_ = key;
-        gexec_len_ = len;
-        ++captures_;
-        if (updated) ++updates_;
+    // the state at the start of the chunk (put back when the grid outgrows its capacity)
+    const int W = y_width<T>(D_);
+    const size_t ny = (size_t) N_ * W, nd = (size_t) N_ * D_;
+    FITSNE_CK(cudaMemcpyAsync(snap_, Y_[cur_], sizeof(T) * ny, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemcpyAsync(snap_ + ny, uY_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemcpyAsync(snap_ + ny + nd, gains_, sizeof(T) * nd, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemcpyAsync(snap_mean_, red_.mean, sizeof(double) * 2, cudaMemcpyDeviceToDevice, st_));
+    FITSNE_CK(cudaMemsetAsync(gstatus_, 0, sizeof(int), st_));
+    // pairs of iterations (the buffers swap twice: one graph per starting buffer serves the
+    // whole chunk), one single iteration for an odd length
+    int c = cur_;
+    for (int k = 0; k < len;) {
+        const int n = (len - k >= 2) ? 2 : 1;
+        rc = launch_iters(p, n, c, k > 0 || mean_pending_);
+        if (rc) return rc;
+        if (n == 1) c = 1 - c;
+        k += n;
     }
+    FITSNE_CK(cudaMemcpyAsync(h_gstat_, gstatus_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    FITSNE_CK(cudaMemcpyAsync(h_gstat_ + 1,
+                              reinterpret_cast<const char *>(dgeom_) + offsetof(DevGeom, g) + offsetof(GridGeom, nb),
+                              sizeof(int), cudaMemcpyDeviceToHost, st_));
     gchunk_cur0_ = cur_;
     gchunk_len_ = len;
-    FITSNE_CK(cudaGraphLaunch(gexec_, st_));
     return 0;
 }
 
 template <typename T>
-std::vector<unsigned long long> Embedding<T>::chunk_key(const UpdateParams &p, int len) const {
+std::vector<unsigned long long> Embedding<T>::iters_key(const UpdateParams &p, int n, int c,
+                                                        bool apply_mean_first) const {
     std::vector<unsigned long long> key;
     auto put = [&key](const void *v, size_t n) {
         unsigned long long w = 0;
         std::memcpy(&w, v, n < 8 ? n : 8);
         key.push_back(w);
     };
-    const bool am = mean_pending_;
-    put(&len, sizeof len);
-    put(&cur_, sizeof cur_);
-    put(&am, sizeof am);
+    put(&n, sizeof n);
+    put(&c, sizeof c);
+    put(&apply_mean_first, sizeof apply_mean_first);
     put(&p.exag, 8);
     put(&p.momentum, 8);
     put(&p.learning_rate, 8);
@@ -1101,11 +1121,13 @@ std::vector<unsigned long long> Embedding<T>::chunk_key(const UpdateParams &p, i
     put(&excl_, sizeof excl_);
     put(&attr_shape_, sizeof attr_shape_);
     put(&fft_thr_, sizeof fft_thr_);
+    put(&tiles_ok_, sizeof tiles_ok_);
+    const void *ord = data_order_ ? (const void *) sorder_ : nullptr;
     for (const void *q : {(const void *) row_, (const void *) col_, (const void *) val_, (const void *) Y_[0],
                           (const void *) Y_[1], (const void *) uY_, (const void *) gains_, (const void *) rep_,
                           (const void *) grid_in_, (const void *) grid_out_, (const void *) work_a_,
                           (const void *) work_b_, (const void *) kspec_, (const void *) tw_dev_, (const void *) trec_,
-                          (const void *) tstart_, (const void *) acc_})
+                          (const void *) tstart_, (const void *) acc_, (const void *) yh_, ord})
         put(&q, sizeof q);
     return key;
 }

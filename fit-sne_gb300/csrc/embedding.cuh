@@ -32,7 +32,7 @@ struct Schedule {
 
 // Embeddings smaller than this are not renumbered (they fit in cache either way).
 constexpr int kReorderMinN = 16384;
-// Longest run of iterations replayed as one CUDA graph.
+// Longest chunk of graph-replayed iterations between two host reads of the grid status.
 constexpr int kMaxChunk = 50;
 
 struct GridParams {
@@ -85,27 +85,36 @@ class Embedding {
     void set_graphs(bool on) { graphs_ = on; }
     bool graphs() const { return graphs_; }
 
-    // ---- graph-captured chunks (used by run_schedule and by the batched driver) ----
-    // A chunk is `len` iterations with constant parameters, recorded on this object's
-    // stream (which must be capturing, or is captured by the caller): snapshot of the state,
-    // then per iteration centre/min-max, device-side grid sizing, spread, convolution,
-    // gather, attraction + update; status and box count copied to pinned memory at the end.
-    int record_chunk(const UpdateParams &p, int len, bool apply_mean_first);
+    // ---- graph-captured chunks (used by run_schedule and by the multi-job driver) ----
+    // A chunk is `len` iterations with constant parameters on this object's stream: a
+    // snapshot of the state, the iterations, then the status and box count copied to pinned
+    // memory.  The iterations are replays of small captured graphs of one or two iterations
+    // each, cached per (iterations, current buffer, mean flag of the first) and captured
+    // again only when what they depend on changes.  A capture and its update cost host time
+    // in proportion to the nodes, with the GPU idle meanwhile: graphs of whole 50-iteration
+    // chunks took 23 ms of a 600-iteration run at N = 1M (9 captures).
+    // record_iters records n iterations starting from buffer c (the stream must be
+    // capturing): per iteration centre/min-max (the first applies the pending mean when
+    // apply_mean_first), device-side grid sizing, spread, convolution, gather, attraction +
+    // update.
+    int record_iters(const UpdateParams &p, int n, int c, bool apply_mean_first);
+    // records (or reuses the cached graph of) n iterations from buffer c and launches it
+    int launch_iters(const UpdateParams &p, int n, int c, bool apply_mean_first);
     // After the chunk ran: 0 ok, 1 the grid outgrew its capacity (state restored: redo the
     // chunk with a larger one), <0 error.  Updates cur_ / mean_pending_ on success.
     int finish_chunk(int len);
     // Capacity for the next chunk from the last known box count (grows buffers; call
     // outside any capture).  grow > 0 forces a larger capacity after an overflow.
     int plan_capacity(int grow);
-    // plan_capacity + record (or reuse the cached graph of) a chunk on this object's stream
-    // and launch it without synchronising; finish_chunk after the stream is idle.
+    // plan_capacity, then the chunk on this object's stream (snapshot, iterations graphs,
+    // status copies) without synchronising; finish_chunk after the stream is idle.
     int launch_chunk(const UpdateParams &p, int len, int grow);
     unsigned long long graph_captures() const { return captures_; }
     unsigned long long graph_updates() const { return updates_; }
     // Runs iterations [it0, it1) with graph chunks; costs may be null.
     int run_schedule_graphs(const Schedule &s, int it0, int it1, double *costs, bool verbose);
-    // What a recorded chunk depends on (parameters, capacity, buffers): equal keys replay.
-    std::vector<unsigned long long> chunk_key(const UpdateParams &p, int len) const;
+    // What recorded iterations depend on (parameters, capacity, buffers): equal keys replay.
+    std::vector<unsigned long long> iters_key(const UpdateParams &p, int n, int c, bool apply_mean_first) const;
     bool mean_pending() const { return mean_pending_; }
     void set_first_geometry() { nb_last_ = geom_.nb; }
     // Renumbering rule of run_schedule (iterations 50, 150, 300, 600 above kReorderMinN).
@@ -223,12 +232,14 @@ class Embedding {
     int nb_cap_ = 0, M_cap_ = 0, L_cap_ = 0, nb_last_ = 0;
     T *snap_ = nullptr;                // state at the start of a chunk: Y, uY, gains
     double *snap_mean_ = nullptr;      // and the pending mean
-    cudaGraphExec_t gexec_ = nullptr;  // cached chunk graph and its key
-    std::vector<unsigned long long> gkey_;
-    int grid_buffers(int M, int L);    // grows grid / FFT buffers to M x M, L
+    struct GraphSlot {  // a cached iterations graph and its key
+        cudaGraphExec_t exec = nullptr;
+        std::vector<unsigned long long> key;
+    };
+    GraphSlot gslots_[2][2][2];     // [iterations - 1][current buffer][mean flag of the first]
+    int grid_buffers(int M, int L);  // grows grid / FFT buffers to M x M, L
     int gchunk_len_ = 0;
     unsigned long long captures_ = 0, updates_ = 0;
-    int gexec_len_ = 0;  // chunk length of the instantiated graph
     int gchunk_cur0_ = 0;
 
     // locality renumbering (reorder.cuh): perm_[k] = caller index of internal point k
