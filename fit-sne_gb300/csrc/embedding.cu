@@ -390,9 +390,15 @@ int Embedding<T>::tune_fft(int M, int L) {
     }
     const char *e = std::getenv("FITSNE_AUTOTUNE");
     if (e && std::atoi(e) == 0) return 0;
+    // one choice per octave of transform lengths: the grid grows through a dozen lengths in
+    // a run, the ranking of the three block sizes stays the same within an octave (N = 1M:
+    // 256 threads ahead at every length from 300 to 864), and each timing costs ~1.5 ms
+    // with the GPU otherwise idle
+    int octave = 0;
+    while ((2 << octave) <= L) ++octave;
     static std::mutex mu;
     static std::map<std::pair<int, int>, int> chosen;
-    const std::pair<int, int> key((int) sizeof(T), L);
+    const std::pair<int, int> key((int) sizeof(T), octave);
     {
         std::lock_guard<std::mutex> lk(mu);
         auto it = chosen.find(key);

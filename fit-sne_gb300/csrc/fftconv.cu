@@ -352,21 +352,33 @@ FITSNE_D void data_cols_body(int kb, int M, const FftPlan &pl, const typename Cx
     const int L = pl.L, H = L / 2 + 1;
     C *spec = reinterpret_cast<C *>(smem_raw);
     C *scratch = spec + 4 * L;
+    // With room for eight transforms (the launch gives 8 L when it fits) the four fields go
+    // through each Stockham stage together: a quarter of the stages' barriers and four times
+    // the butterflies per stage for the block's threads.  Otherwise one field at a time with
+    // one transform of scratch.  The butterflies are the same either way.
+    unsigned dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    const bool wide = (size_t) dyn >= 8 * (size_t) L * sizeof(C);
     for (int f = 0; f < 4; ++f)
         for (int a = threadIdx.x; a < L; a += blockDim.x)
             spec[f * L + a] = (a < M) ? d1[((size_t) f * M + a) * H + kb] : mkc(T(0), T(0));
     __syncthreads();
-    for (int f = 0; f < 4; ++f) {
-        C *res = fft_block(spec + f * L, scratch, 1, pl, tw, false);
-        if (res != spec + f * L) {
-            for (int a = threadIdx.x; a < L; a += blockDim.x) spec[f * L + a] = res[a];
-            __syncthreads();
+    C *fw = spec;  // the four forward spectra
+    if (wide) {
+        fw = fft_block(spec, scratch, 4, pl, tw, false);
+    } else {
+        for (int f = 0; f < 4; ++f) {
+            C *res = fft_block(spec + f * L, scratch, 1, pl, tw, false);
+            if (res != spec + f * L) {
+                for (int a = threadIdx.x; a < L; a += blockDim.x) spec[f * L + a] = res[a];
+                __syncthreads();
+            }
         }
     }
     // spectral products forming V1, Rx, Ry and S (df = 1) or Vgen (variable df)
     for (int ka = threadIdx.x; ka < L; ka += blockDim.x) {
         const KSpec<T> e = kspec[(size_t) kb * L + ka];
-        const C w1 = spec[ka], w2 = spec[L + ka], w3 = spec[2 * L + ka], w4 = spec[3 * L + ka];
+        const C w1 = fw[ka], w2 = fw[L + ka], w3 = fw[2 * L + ka], w4 = fw[3 * L + ka];
         // (i g) w = (-g w.y, g w.x)
         const C gxw1 = mkc(-e.gx * w1.y, e.gx * w1.x);
         const C gyw1 = mkc(-e.gy * w1.y, e.gy * w1.x);
@@ -381,17 +393,30 @@ FITSNE_D void data_cols_body(int kb, int M, const FftPlan &pl, const typename Cx
         } else {
             s4 = cscale(w1, e.h);
         }
-        spec[ka] = v1;
-        spec[L + ka] = rx;
-        spec[2 * L + ka] = ry;
-        spec[3 * L + ka] = s4;
+        fw[ka] = v1;
+        fw[L + ka] = rx;
+        fw[2 * L + ka] = ry;
+        fw[3 * L + ka] = s4;
     }
     __syncthreads();
+    if (wide) {
+        const C *res = fft_block(fw, fw == spec ? scratch : spec, 4, pl, tw, true);
+        for (int f = 0; f < 4; ++f)
+            for (int a = threadIdx.x; a < M; a += blockDim.x) d2[((size_t) f * M + a) * H + kb] = res[f * L + a];
+        return;
+    }
     for (int f = 0; f < 4; ++f) {
         C *res = fft_block(spec + f * L, scratch, 1, pl, tw, true);
         for (int a = threadIdx.x; a < M; a += blockDim.x) d2[((size_t) f * M + a) * H + kb] = res[a];
         __syncthreads();
     }
+}
+
+// shared memory of the column pass: eight transforms when they fit (the four fields together)
+template <typename C>
+size_t data_cols_smem(int L) {
+    const size_t s8 = 8 * (size_t) L * sizeof(C);
+    return s8 <= 227 * 1024 ? s8 : 5 * (size_t) L * sizeof(C);
 }
 
 template <typename T>
@@ -553,14 +578,15 @@ cudaError_t conv2d_launch(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M, co
     if ((e = set_smem(k_kernel_rows<T>, s4)) != cudaSuccess) return e;
     if ((e = set_smem(k_kernel_cols<T>, s5)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_rows<T>, s4)) != cudaSuccess) return e;
-    if ((e = set_smem(k_data_cols<T>, s5)) != cudaSuccess) return e;
+    const size_t sc = data_cols_smem<C>(L);
+    if ((e = set_smem(k_data_cols<T>, sc)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
     const int thr = (threads >= 32 && threads <= 1024 && threads % 32 == 0) ? threads : 256;
     // kernel spectra: krow uses work_a ([4][L][H]); data passes use work_b ([4][M][H]) then work_a
     k_kernel_rows<T><<<M, thr, s4, st>>>(M, plan, tw, work_a, (T) h, (T) df, mode, nullptr);
     k_kernel_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_a, kspec, nullptr);
     k_data_rows<T><<<M, thr, s4, st>>>(grid_in, M, plan, tw, work_b, nullptr);
-    k_data_cols<T><<<H, thr, s5, st>>>(M, plan, tw, work_b, kspec, work_a, mode, nullptr);
+    k_data_cols<T><<<H, thr, sc, st>>>(M, plan, tw, work_b, kspec, work_a, mode, nullptr);
     k_data_rows_inv<T><<<M, thr, s4, st>>>(work_a, M, plan, tw, grid_out, nullptr);
     return cudaGetLastError();
 }
@@ -578,14 +604,15 @@ cudaError_t conv2d_launch_dev(const Cell4<T> *grid_in, Cell4<T> *grid_out, int M
     if ((e = set_smem(k_kernel_rows<T>, s4)) != cudaSuccess) return e;
     if ((e = set_smem(k_kernel_cols<T>, s5)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_rows<T>, s4)) != cudaSuccess) return e;
-    if ((e = set_smem(k_data_cols<T>, s5)) != cudaSuccess) return e;
+    const size_t sc = data_cols_smem<C>(L_cap);
+    if ((e = set_smem(k_data_cols<T>, sc)) != cudaSuccess) return e;
     if ((e = set_smem(k_data_rows_inv<T>, s4)) != cudaSuccess) return e;
     const int thr = (threads >= 32 && threads <= 1024 && threads % 32 == 0) ? threads : 256;
     FftPlan dummy{};
     k_kernel_rows<T><<<M_cap, thr, s4, st>>>(0, dummy, tw, work_a, T(0), (T) df, mode, cg);
     k_kernel_cols<T><<<H, thr, s5, st>>>(0, dummy, tw, work_a, kspec, cg);
     k_data_rows<T><<<M_cap, thr, s4, st>>>(grid_in, 0, dummy, tw, work_b, cg);
-    k_data_cols<T><<<H, thr, s5, st>>>(0, dummy, tw, work_b, kspec, work_a, mode, cg);
+    k_data_cols<T><<<H, thr, sc, st>>>(0, dummy, tw, work_b, kspec, work_a, mode, cg);
     k_data_rows_inv<T><<<M_cap, thr, s4, st>>>(work_a, 0, dummy, tw, grid_out, cg);
     return cudaGetLastError();
 }
@@ -732,13 +759,14 @@ cudaError_t conv2d_launch_batch(const Cell4<T> *grid_in, Cell4<T> *grid_out, con
     if ((e = set_smem(k_bkernel_rows<T>, s4)) != cudaSuccess) return e;
     if ((e = set_smem(k_bkernel_cols<T>, s5)) != cudaSuccess) return e;
     if ((e = set_smem(k_bdata_rows<T>, s4)) != cudaSuccess) return e;
-    if ((e = set_smem(k_bdata_cols<T>, s5)) != cudaSuccess) return e;
+    const size_t sc = data_cols_smem<C>(L_max);
+    if ((e = set_smem(k_bdata_cols<T>, sc)) != cudaSuccess) return e;
     if ((e = set_smem(k_bdata_rows_inv<T>, s4)) != cudaSuccess) return e;
     const int thr = 256;
     k_bkernel_rows<T><<<nkrow, thr, s4, st>>>(krow, jobs, tw, work_a, (T) df, mode);
     k_bkernel_cols<T><<<ncols, thr, s5, st>>>(cols, jobs, tw, work_a, kspec);
     k_bdata_rows<T><<<nrows, thr, s4, st>>>(rows, jobs, grid_in, tw, work_b);
-    k_bdata_cols<T><<<ncols, thr, s5, st>>>(cols, jobs, tw, work_b, kspec, work_a, mode);
+    k_bdata_cols<T><<<ncols, thr, sc, st>>>(cols, jobs, tw, work_b, kspec, work_a, mode);
     k_bdata_rows_inv<T><<<nrows, thr, s4, st>>>(rows, jobs, work_a, tw, grid_out);
     return cudaGetLastError();
 }

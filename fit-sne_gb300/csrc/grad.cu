@@ -1243,11 +1243,16 @@ FITSNE_D void kl_body(const uint32_t *__restrict__ row, const uint32_t *__restri
     const T zinv = T(1.0 / *r.z);
     const T df = T(dfd);
     const T ex = T(exag);
+    const bool df1 = dfd == 1.0;
     double acc[1] = {0.0};
     for (int i = row0 + gw; i < row0 + N; i += nw) {
         P ci[D];
         YL<T, D>::load(Y, i, ci);
         const uint32_t e1 = row[i + 1];
+        // FP32 form: a lane's terms of the row (about five) add up in FP32, then once into
+        // the FP64 sum (one conversion and FP64 add per row and lane instead of per edge; the
+        // FP64 pipe runs at a small fraction of the FP32 rate)
+        T racc = T(0);
         for (uint32_t e = row[i] + lane; e < e1; e += 32) {
             P cj[D];
             YL<T, D>::load(Y, (int) col[e], cj);
@@ -1257,11 +1262,17 @@ FITSNE_D void kl_body(const uint32_t *__restrict__ row, const uint32_t *__restri
                 const T dx = pdiff(ci[d], cj[d]);
                 d2 += dx * dx;
             }
-            const T base = T(1) / (T(1) + d2 / df);
-            const T Q = (dfd == 1.0 ? base : pow(base, df)) * zinv;
+            // 1 / (1 + d2 / df), the same value in fewer instructions for df = 1
+            const T base = df1 ? recip(T(1) + d2) : T(1) / (T(1) + d2 / df);
+            const T Q = (df1 ? base : pow(base, df)) * zinv;
             const T pv = val[e] * ex;
-            acc[0] += (double) (pv * log((pv + T(FLT_MIN)) / (Q + T(FLT_MIN))));
+            const T term = pv * log((pv + T(FLT_MIN)) / (Q + T(FLT_MIN)));
+            if constexpr (sizeof(T) == 4)
+                racc += term;
+            else
+                acc[0] += (double) term;
         }
+        if constexpr (sizeof(T) == 4) acc[0] += (double) racc;
     }
     if (grid_sum<1>(acc, r.part, r.count + 3, sh, blk, nblk)) *r.kl = acc[0];
 }
