@@ -211,11 +211,9 @@ FITSNE_D void block_sum(double (&v)[NV], double *sh) {
     __syncthreads();
 }
 
-// Writes this block's partials; returns true in thread 0 of the last block to finish,
-// with v replaced by the total over all blocks (summed in block order).
+// Second half of grid_sum: thread 0 holds the block's sums in v.
 template <int NV>
-FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, double *sh, int blk, int nblk) {
-    block_sum<NV>(v, sh);
+FITSNE_D bool grid_sum_finish(double (&v)[NV], double *part, unsigned int *count, double *sh, int blk, int nblk) {
     __shared__ bool last;
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -243,25 +241,51 @@ FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, doubl
     return false;
 }
 
-// min / max with the same rule as the reference
+// Writes this block's partials; returns true in thread 0 of the last block to finish,
+// with v replaced by the total over all blocks.
 template <int NV>
-FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *count, double *sh, int blk, int nblk) {
+FITSNE_D bool grid_sum(double (&v)[NV], double *part, unsigned int *count, double *sh, int blk, int nblk) {
+    block_sum<NV>(v, sh);
+    return grid_sum_finish<NV>(v, part, count, sh, blk, nblk);
+}
+
+// The block's sums of double-float values in double-float arithmetic (FP32 pipe), into out
+// (FP64) in thread 0: one conversion a block instead of FP64 shuffles and adds in every warp
+// (the FP64 pipe takes ~16 cycles a warp instruction; the attraction's warps all reach their
+// mean reduction at the end of the launch).  sh holds NV doubles per warp.
+template <int NV>
+FITSNE_D void block_sum_df(df32 (&v)[NV], double (&out)[NV], double *sh) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = 16; o; o >>= 1) {
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
-    if (lane == 0) {
-        sh[2 * wid] = mn;
-        sh[2 * wid + 1] = mx;
+    float *shf = reinterpret_cast<float *>(sh);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        df32 x = v[k];
+        for (int o = 16; o; o >>= 1) x = df_add(x, df32{__shfl_xor_sync(full, x.hi, o), __shfl_xor_sync(full, x.lo, o)});
+        if (lane == 0) {
+            shf[2 * (wid * NV + k)] = x.hi;
+            shf[2 * (wid * NV + k) + 1] = x.lo;
+        }
     }
     __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            df32 x{0.f, 0.f};
+            for (int w = 0; w < nw; ++w) x = df_add(x, df32{shf[2 * (w * NV + k)], shf[2 * (w * NV + k) + 1]});
+            out[k] = df_to_double(x);
+        }
+    }
+    __syncthreads();
+}
+
+// grid min / max, second half: thread 0 holds the block's (mn, mx); the last block to finish
+// combines the blocks' values and returns true in its thread 0
+FITSNE_D bool grid_minmax_finish(double &mn, double &mx, double *part, unsigned int *count, double *sh, int blk,
+                                 int nblk) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     __shared__ bool last;
     if (threadIdx.x == 0) {
-        for (int w = 1; w < nw; ++w) {
-            mn = fmin(mn, sh[2 * w]);
-            mx = fmax(mx, sh[2 * w + 1]);
-        }
         part[2 * blk] = mn;
         part[2 * blk + 1] = mx;
         __threadfence();
@@ -297,6 +321,73 @@ FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *co
         return true;
     }
     return false;
+}
+
+// min / max with the same rule as the reference (FP64 values per thread)
+FITSNE_D bool grid_minmax(double &mn, double &mx, double *part, unsigned int *count, double *sh, int blk, int nblk) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane == 0) {
+        sh[2 * wid] = mn;
+        sh[2 * wid + 1] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w) {
+            mn = fmin(mn, sh[2 * w]);
+            mx = fmax(mx, sh[2 * w + 1]);
+        }
+    }
+    __syncthreads();  // sh is reused by the finish
+    return grid_minmax_finish(mn, mx, part, count, sh, blk, nblk);
+}
+
+// FP32 form: the same over double-float values ordered by their (hi, lo) pairs, reduced within
+// the block in FP32 (shuffles and compares) and converted to FP64 once per block; the FP64
+// pipe takes ~16 cycles a warp instruction, which the per-warp FP64 reductions of 1,216
+// blocks paid in every iteration.  (double) hi + (double) lo is exact, so the result is the
+// FP64 reduction's.
+FITSNE_D void pair_min(float &h, float &l, float h2, float l2) {
+    if (h2 < h || (h2 == h && l2 < l)) {
+        h = h2;
+        l = l2;
+    }
+}
+FITSNE_D void pair_max(float &h, float &l, float h2, float l2) {
+    if (h2 > h || (h2 == h && l2 > l)) {
+        h = h2;
+        l = l2;
+    }
+}
+FITSNE_D bool grid_minmax_pairs(float nh, float nl, float xh, float xl, double &mn, double &mx, double *part,
+                                unsigned int *count, double *sh, int blk, int nblk) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o; o >>= 1) {
+        pair_min(nh, nl, __shfl_xor_sync(full, nh, o), __shfl_xor_sync(full, nl, o));
+        pair_max(xh, xl, __shfl_xor_sync(full, xh, o), __shfl_xor_sync(full, xl, o));
+    }
+    float *shf = reinterpret_cast<float *>(sh);  // 4 floats per warp (sh holds 2 doubles a warp)
+    if (lane == 0) {
+        shf[4 * wid] = nh;
+        shf[4 * wid + 1] = nl;
+        shf[4 * wid + 2] = xh;
+        shf[4 * wid + 3] = xl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nw; ++w) {
+            pair_min(nh, nl, shf[4 * w], shf[4 * w + 1]);
+            pair_max(xh, xl, shf[4 * w + 2], shf[4 * w + 3]);
+        }
+        mn = (double) nh + (double) nl;
+        mx = (double) xh + (double) xl;
+    }
+    __syncthreads();  // sh is reused by the finish
+    return grid_minmax_finish(mn, mx, part, count, sh, blk, nblk);
 }
 
 // ---------------------------------------------------------------------------------
@@ -348,11 +439,12 @@ FITSNE_D void center_minmax_body(T *Y, int N, int apply_mean, int excl, RedScrat
             }
         }
     }
-    if constexpr (sizeof(T) == 4) {
-        mn = (double) nh + (double) nl;
-        mx = (double) xh + (double) xl;
-    }
-    if (grid_minmax<2>(mn, mx, r.part, r.count + 0, sh, blk, nblk)) {
+    bool done;
+    if constexpr (sizeof(T) == 4)
+        done = grid_minmax_pairs(nh, nl, xh, xl, mn, mx, r.part, r.count + 0, sh, blk, nblk);
+    else
+        done = grid_minmax(mn, mx, r.part, r.count + 0, sh, blk, nblk);
+    if (done) {
         r.mnmx[0] = mn;
         r.mnmx[1] = mx;
     }
@@ -712,9 +804,17 @@ FITSNE_D void attr_finish(int lane, unsigned int nwarps, int N, const UpdatePara
     }
     if (p.mode != 0) {
         double m[2] = {0.0, 0.0};
+        bool done;
+        if constexpr (sizeof(T) == 4) {
+            df32 v[2] = {msum[0], D == 2 ? msum[D - 1] : df32{0.f, 0.f}};
+            block_sum_df<2>(v, m, sh);
+            done = grid_sum_finish<2>(m, r.part, r.count + 2, sh, blk, nblk);
+        } else {
 #pragma unroll
-        for (int d = 0; d < D; ++d) m[d] = ptod(msum[d]);
-        if (grid_sum<2>(m, r.part, r.count + 2, sh, blk, nblk)) {
+            for (int d = 0; d < D; ++d) m[d] = ptod(msum[d]);
+            done = grid_sum<2>(m, r.part, r.count + 2, sh, blk, nblk);
+        }
+        if (done) {
             r.mean[0] = m[0] / (double) N;
             r.mean[1] = m[1] / (double) N;
         }
@@ -1018,9 +1118,9 @@ __global__ void __launch_bounds__(kBlock)
     }
     if (p.mode != 0) {
         double m[2] = {0.0, 0.0};
-#pragma unroll
-        for (int d = 0; d < D; ++d) m[d] = ptod(msum[d]);
-        if (grid_sum<2>(m, r.part, r.count + 2, sh, blockIdx.x, gridDim.x)) {
+        df32 v[2] = {msum[0], D == 2 ? msum[D - 1] : df32{0.f, 0.f}};
+        block_sum_df<2>(v, m, sh);
+        if (grid_sum_finish<2>(m, r.part, r.count + 2, sh, blockIdx.x, gridDim.x)) {
             r.mean[0] = m[0] / (double) N;
             r.mean[1] = m[1] / (double) N;
         }
