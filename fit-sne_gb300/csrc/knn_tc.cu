@@ -297,15 +297,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             // lower bound on d^2 between the query tile's sphere and a sphere (centre t of
             // centT, radius rr), less nothing: the callers subtract the error bound of the split
             // distances
-            auto lower_bound2 = [&](const float *__restrict__ centT, int ntiles, int t, float rr,
-                                    float *centre_d2 = nullptr) {
+            auto lower_bound2 = [&](const float *__restrict__ centT, int ntiles, int t, float rr) {
                 float dd = 0.f;
 #pragma unroll 8
                 for (int d = 0; d < D; ++d) {
                     const float e = qc_s[d] - centT[(size_t) d * ntiles + t];
                     dd = fmaf(e, e, dd);
                 }
-                if (centre_d2) *centre_d2 = dd;
                 const float lb = fmaxf(0.f, sqrtf(dd) * (1.f - 1e-5f) - rq - rr);
                 return lb * lb * (1.f - 1e-5f);
             };
@@ -381,26 +379,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const int rtc = rt < nRT ? rt : nRT - 1;
                     const float rr = rt < nRT ? rrad[rtc] : -1.f;
                     const float thr_t = threshold();
-                    float cd2 = 0.f;
-                    const float lb2 = rr >= 0.f ? lower_bound2(rcentT, nRT, rtc, rr, &cd2) : 0.f;
-                    const bool keep = rr >= 0.f && !(thr_t < FLT_MAX && lb2 - errm > thr_t);
-                    // the kept tiles of these 32 nearest centre first (the lane in the low five
-                    // bits): the lists' thresholds fall sooner, so fewer later columns pass
-                    // them and enter the heaps.  The order changes no list, only the work.
-                    uint32_t key = keep ? ((__float_as_uint(cd2) & ~31u) | (uint32_t) lane) : 0xffffffffu;
-#pragma unroll
-                    for (int size = 2; size <= 32; size <<= 1)
-#pragma unroll
-                        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                            const uint32_t o = __shfl_xor_sync(0xffffffffu, key, stride);
-                            const bool up = (lane & size) == 0, lower = (lane & stride) == 0;
-                            key = (lower == up) ? min(key, o) : max(key, o);
-                        }
-                    for (int q = 0; q < 32 && ok; ++q) {
-                        const uint32_t kq = __shfl_sync(0xffffffffu, key, q);
-                        if (kq == 0xffffffffu) break;
+                    const bool keep =
+                        rr >= 0.f && !(thr_t < FLT_MAX && lower_bound2(rcentT, nRT, rtc, rr) - errm > thr_t);
+                    uint32_t tmask = __ballot_sync(0xffffffffu, keep);
+                    while (tmask && ok) {
+                        const int tl = __ffs(tmask) - 1;
+                        tmask &= tmask - 1;
                         ++kept;
-                        issue(sbk * SBT + ((c + (int) (kq & 31u) + r) & (SBT - 1)));
+                        issue(sbk * SBT + ((c + tl + r) & (SBT - 1)));
                     }
                 }
             }
