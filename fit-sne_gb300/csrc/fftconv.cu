@@ -11,6 +11,8 @@
 // Every pass keeps one or two whole transforms in shared memory; passes are Stockham
 // (self-sorting) with radix 4, 2, 3, 5 butterflies.
 #include <climits>
+#include <map>
+#include <mutex>
 
 #include "fftconv.cuh"
 
@@ -558,9 +560,20 @@ __global__ void k_conv1d_inv(const typename Cx<T>::t *__restrict__ work, int M, 
     }
 }
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`, never lowers it: a launch
+// recorded earlier in a CUDA graph for a larger transform (the iteration graphs are sized for
+// the grid capacity) must stay valid after a smaller direct launch (the host-path step, the
+// block-size timing), including when a profiler replays the graph's kernels one by one.
 template <typename K>
 cudaError_t set_smem(K kernel, size_t bytes) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+    static std::mutex mu;
+    static std::map<const void *, size_t> limit;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &cur = limit[reinterpret_cast<const void *>(kernel)];
+    if (bytes <= cur || bytes <= 48 * 1024) return cudaSuccess;  // 48 KB need no attribute
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
 }
 
 }  // namespace
