@@ -101,11 +101,11 @@ struct BoxP<double> {
 };
 
 __host__ __device__ BoxP<float> make_box(const GridGeom &g, float *) {
-    BoxP<float> b;
-    b.neg_mn = df_from_double(-g.mn);
-    b.bw = df_from_double(g.bw);
-    b.inv_bw = (float) (1.0 / g.bw);
-    b.bwT = (float) g.bw;
+    BoxP<float> b;  // the FP32 values as grid_geom made them (df_from_double, 1 / bw)
+    b.neg_mn = {g.neg_mn32[0], g.neg_mn32[1]};
+    b.bw = {g.bw32[0], g.bw32[1]};
+    b.inv_bw = g.inv_bw32;
+    b.bwT = g.bw32[0];
     b.mn64 = g.mn;
     b.bw64 = g.bw;
     b.nb = g.nb;
@@ -395,15 +395,22 @@ FITSNE_D bool grid_minmax_pairs(float nh, float nl, float xh, float xl, double &
 template <typename T, int D>
 FITSNE_D void center_minmax_body(T *Y, int N, int apply_mean, int excl, RedScratch r, double *sh, int blk, int nblk) {
     typedef typename YL<T, D>::P P;
+    // -mean in the positions' form, made by thread 0 (FP64 conversions: see step_scalars)
+    __shared__ P s_negm[D];
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const double m = apply_mean ? r.mean[d] : 0.0;
+            if constexpr (sizeof(T) == 4)
+                s_negm[d] = df_from_double(-m);
+            else
+                s_negm[d] = -m;
+        }
+    }
+    __syncthreads();
     P negm[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) {
-        const double m = apply_mean ? r.mean[d] : 0.0;
-        if constexpr (sizeof(T) == 4)
-            negm[d] = df_from_double(-m);
-        else
-            negm[d] = -m;
-    }
+    for (int d = 0; d < D; ++d) negm[d] = s_negm[d];
     double mn = HUGE_VAL, mx = -HUGE_VAL;
     // FP32 form: the double-float values compared by their (hi, lo) pairs, whose order is the
     // values' order for normalised pairs (hi = fl(hi + lo)), so the thread's min / max cost one
@@ -598,16 +605,24 @@ FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<fl
             if (lane < NV) {
                 const long long off = (long long) (lane / NT) * b.M + lane % NT;
                 float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                for (int pt = 0; pt < 32; ++pt) {
-                    const float4 x = wb->v[lane][pt];
-                    acc.x += x.x;
-                    acc.y += x.y;
-                    acc.z += x.z;
-                    acc.w += x.w;
-                    if ((ends >> pt) & 1u) {
-                        const long long c = wb->cell[pt];
-                        if (c >= 0) atomicAdd(reinterpret_cast<float4 *>(grid + c + off), acc);
-                        acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                // eight points' loads issued together, then added in order: one shared-memory
+                // latency per eight points instead of per point
+#pragma unroll 1
+                for (int g = 0; g < 32; g += 8) {
+                    float4 x[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) x[k] = wb->v[lane][g + k];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        acc.x += x[k].x;
+                        acc.y += x[k].y;
+                        acc.z += x[k].z;
+                        acc.w += x[k].w;
+                        if ((ends >> (g + k)) & 1u) {
+                            const long long c = wb->cell[g + k];
+                            if (c >= 0) atomicAdd(reinterpret_cast<float4 *>(grid + c + off), acc);
+                            acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
                     }
                 }
             }
@@ -734,14 +749,42 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 // repulsion over Z; tsne.cpp:1121-1155) and, in mode 1, the reference's update (gains,
 // momentum, step clipping; tsne.cpp:479-531) into Yout, the new position added to msum; in
 // mode 0 the gradient into dC only.
+// The step's scalars in the kernel's type, made once per block by thread 0 (the FP64
+// division and conversions cost every warp that made them ~16 cycles a warp instruction on
+// GB300's FP64 pipe, all at the start of the launch).  Called by every thread of the block.
+template <typename T>
+struct StepScalars {
+    T zinv, exag, df, momentum, lr, max_step;
+    bool df1, clip;
+};
+template <typename T>
+FITSNE_D StepScalars<T> step_scalars(const UpdateParams &p, const double *z) {
+    __shared__ StepScalars<T> sc;
+    if (threadIdx.x == 0) {
+        sc.zinv = T(1.0 / *z);
+        sc.exag = T(p.exag);
+        sc.df = T(p.df);
+        sc.momentum = T(p.momentum);
+        sc.lr = T(p.learning_rate);
+        sc.max_step = T(p.max_step_norm);
+        sc.df1 = p.df == 1.0;
+        sc.clip = p.max_step_norm > 0;
+    }
+    __syncthreads();
+    const StepScalars<T> v = sc;
+    __syncthreads();  // a later call may rewrite sc
+    return v;
+}
+
 template <typename T, int D>
 FITSNE_D void attr_row_update(int my, const T (&amy)[D], const typename YL<T, D>::P (&cmy)[D], const UpdateParams &p,
-                              T zinv, T exag, const T *__restrict__ rep, T *__restrict__ dC, T *__restrict__ gains,
-                              T *__restrict__ uY, T *__restrict__ Yout, typename YL<T, D>::P (&msum)[D]) {
+                              const StepScalars<T> &sc, const T *__restrict__ rep, T *__restrict__ dC,
+                              T *__restrict__ gains, T *__restrict__ uY, T *__restrict__ Yout,
+                              typename YL<T, D>::P (&msum)[D]) {
     typedef typename YL<T, D>::P P;
     T gr[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) gr[d] = exag * amy[d] - rep[(size_t) my * D + d] * zinv;
+    for (int d = 0; d < D; ++d) gr[d] = sc.exag * amy[d] - rep[(size_t) my * D + d] * sc.zinv;
     if (p.mode == 0) {
 #pragma unroll
         for (int d = 0; d < D; ++d) dC[(size_t) my * D + d] = gr[d];
@@ -758,15 +801,15 @@ FITSNE_D void attr_row_update(int my, const T (&amy)[D], const typename YL<T, D>
             gn = (sgn(gr[d]) != sgn(uo)) ? (gn + T(0.2)) : (gn * T(0.8));
             if (gn < T(0.01)) gn = T(0.01);
             gains[(size_t) my * D + d] = gn;
-            u[d] = T(p.momentum) * uo - T(p.learning_rate) * gn * gr[d];
+            u[d] = sc.momentum * uo - sc.lr * gn * gr[d];
             nrm2 += u[d] * u[d];
         }
-        if (p.max_step_norm > 0) {
+        if (sc.clip) {
             const T step = sqrt(nrm2);
-            if (step > T(p.max_step_norm)) {
-                const T sc = T(p.max_step_norm) / step;
+            if (step > sc.max_step) {
+                const T f = sc.max_step / step;
 #pragma unroll
-                for (int d = 0; d < D; ++d) u[d] *= sc;
+                for (int d = 0; d < D; ++d) u[d] *= f;
             }
         }
 #pragma unroll
@@ -845,11 +888,9 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
     const int lane = threadIdx.x & 31;
     const int ngroups = (N + kAttrGroup - 1) / kAttrGroup;
     const unsigned int nwarps = (nblk * blockDim.x) >> 5;
-    const double Zd = *r.z;
-    const T zinv = T(1.0 / Zd);
-    const T df = T(p.df);
-    const bool df1 = (p.df == 1.0);
-    const T exag = T(p.exag);
+    const StepScalars<T> sc = step_scalars<T>(p, r.z);
+    const T df = sc.df;
+    const bool df1 = sc.df1;
     P msum[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -994,7 +1035,7 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
             }
         }
         if (!live) continue;
-        attr_row_update<T, D>(my, amy, cmy, p, zinv, exag, rep, dC, gains, uY, Yout, msum);
+        attr_row_update<T, D>(my, amy, cmy, p, sc, rep, dC, gains, uY, Yout, msum);
     }
     attr_finish<T, D>(lane, nwarps, N, p, r, msum, sh, blk, nblk);
 }
@@ -1096,8 +1137,7 @@ __global__ void __launch_bounds__(kBlock)
                  const float *__restrict__ rep, int N, UpdateParams p, RedScratch r) {
     __shared__ double sh[2 * 32];
     typedef df32 P;
-    const float zinv = (float) (1.0 / *r.z);
-    const float exag = (float) p.exag;
+    const StepScalars<float> sc = step_scalars<float>(p, r.z);
     P msum[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) msum[d] = {0.f, 0.f};
@@ -1114,7 +1154,7 @@ __global__ void __launch_bounds__(kBlock)
         }
         P cmy[D];
         YL<float, D>::load(Yin, i, cmy);
-        attr_row_update<float, D>(i, amy, cmy, p, zinv, exag, rep, dC, gains, uY, Yout, msum);
+        attr_row_update<float, D>(i, amy, cmy, p, sc, rep, dC, gains, uY, Yout, msum);
     }
     if (p.mode != 0) {
         double m[2] = {0.0, 0.0};

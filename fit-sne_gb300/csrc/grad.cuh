@@ -38,6 +38,11 @@ struct GridGeom {
     double hk;      // node spacing used for the kernel samples (box width / nterms)
     float s32[kMaxInterp], inv_den32[kMaxInterp];
     double s64[kMaxInterp], inv_den64[kMaxInterp];
+    // FP32 forms for the FP32 kernels: -mn and bw as double-float (hi, lo) pairs, 1 / bw
+    // rounded to float.  Made once here: every thread of the spread and gather used to derive
+    // them itself, ~20 FP64-pipe instructions a warp at ~16 cycles each (about 30 us a launch
+    // over 31,250 warps at N = 1M).
+    float neg_mn32[2], bw32[2], inv_bw32;
 };
 
 // The reference's grid rule (computeFftGradient*, tsne.cpp:769-780, 1039-1077; box bounds
@@ -91,6 +96,12 @@ FITSNE_HD GridGeom grid_geom(double mn, double mx, int D, int nterms, double ipi
         g.s32[i] = (float) s[i];
         g.inv_den32[i] = (float) (1.0 / den);
     }
+    const double nm = -g.mn;
+    g.neg_mn32[0] = (float) nm;
+    g.neg_mn32[1] = (float) (nm - (double) g.neg_mn32[0]);
+    g.bw32[0] = (float) g.bw;
+    g.bw32[1] = (float) (g.bw - (double) g.bw32[0]);
+    g.inv_bw32 = (float) (1.0 / g.bw);
     return g;
 }
 
