@@ -60,6 +60,15 @@ def test_run_random_init_uses_the_reference_generator(gpu_lib):
     assert np.allclose(Y.ravel(), out, rtol=1e-14, atol=0)
 
 
+def test_run_leaves_the_data_unmodified(gpu_lib):
+    """fitsne_run reads X without centring or rescaling it in place (the reference does both to
+    its own copy), so the wrapper passes the caller's array without copying it."""
+    X = np.random.default_rng(1).standard_normal((500, 6)) * 3.0 + 1.0
+    X0 = X.copy()
+    gpu_lib.run(X, perplexity=10.0, rand_seed=3, max_iter=5)
+    assert np.array_equal(X, X0)
+
+
 @pytest.mark.parametrize("case", ["late_exag_1d_df05", "no_momentum_2d", "auto_exag", "perp_list_df3"])
 def test_run_options_match_restatement(gpu_lib, orc, case):
     rng = np.random.default_rng(11)
