@@ -877,7 +877,12 @@ FITSNE_D void attr_finish(int lane, unsigned int nwarps, int N, const UpdatePara
 // batch: all index / value loads first, then all gathers.
 // Rows [row0, row0 + N) of the CSR (column indices and Y are global); blk / nblk: this
 // block's index among the nblk blocks that share the rows (and r's counters).
-template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups, bool kPipe>
+// kKL: the same traversal evaluates the KL divergence instead (evaluateErrorFft,
+// tsne.cpp:1329-1355): per edge val * exag * log((val * exag + FLT_MIN) / (Q + FLT_MIN)) with
+// Q = q^df / Z (p.exag the multiplier, *r.z the Z of the last gradient, full positions: yh
+// null), a lane's terms of a row summed in FP32 and added to its FP64 sum once per row, the
+// grid sum into *r.kl; no update.
+template <typename T, int D, int kAttrGroup, int kAttrUnroll, bool kBlockGroups, bool kPipe, bool kKL = false>
 FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
                         const T *__restrict__ val, const T *__restrict__ Yin, T *__restrict__ Yout,
                         T *__restrict__ uY, T *__restrict__ gains, T *__restrict__ dC, const T *__restrict__ rep,
@@ -899,6 +904,7 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
         else
             msum[d] = 0.0;
     }
+    double klsum[1] = {0.0};  // kKL: this lane's terms
     while (true) {
         int g = 0;
         if constexpr (kBlockGroups) {
@@ -1023,10 +1029,20 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
                         d2 += dx[d] * dx[d];
                     }
                     const T q = recip(df1 ? T(1) + d2 : T(1) + d2 / df);
-                    const T vq = v[u] * q;
+                    if constexpr (kKL) {
+                        const T Q = (df1 ? q : pow(q, df)) * sc.zinv;
+                        const T pv = v[u] * sc.exag;
+                        a[0] += pv * log((pv + T(FLT_MIN)) / (Q + T(FLT_MIN)));  // 0 past the row
+                    } else {
+                        const T vq = v[u] * q;
 #pragma unroll
-                    for (int d = 0; d < D; ++d) a[d] += vq * dx[d];
+                        for (int d = 0; d < D; ++d) a[d] += vq * dx[d];
+                    }
                 }
+            }
+            if constexpr (kKL) {
+                klsum[0] += (double) a[0];  // FP32 form: the row's terms of this lane, once
+                continue;
             }
 #pragma unroll
             for (int d = 0; d < D; ++d) {
@@ -1034,8 +1050,20 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
                 if (lane == k) amy[d] = a[d];
             }
         }
-        if (!live) continue;
+        if (kKL || !live) continue;
         attr_row_update<T, D>(my, amy, cmy, p, sc, rep, dC, gains, uY, Yout, msum);
+    }
+    if constexpr (kKL) {
+        if (lane == 0) {  // the work counter's reset, as attr_finish does it
+            __threadfence();
+            const unsigned int out = atomicAdd(r.count + 5, 1u);
+            if (out == nwarps - 1) {
+                atomicExch(r.count + 4, 0u);
+                atomicExch(r.count + 5, 0u);
+            }
+        }
+        if (grid_sum<1>(klsum, r.part, r.count + 3, sh, blk, nblk)) *r.kl = klsum[0];
+        return;
     }
     attr_finish<T, D>(lane, nwarps, N, p, r, msum, sh, blk, nblk);
 }
@@ -1417,12 +1445,17 @@ FITSNE_D void kl_body(const uint32_t *__restrict__ row, const uint32_t *__restri
     if (grid_sum<1>(acc, r.part, r.count + 3, sh, blk, nblk)) *r.kl = acc[0];
 }
 
+// KL over the CSR in the attraction's traversal (groups of 16 rows from the work counter, two
+// edges per lane per batch, the next row's CSR lines prefetched): 1.15 ms at N = 1M with a warp
+// per row and lanes striding its edges.  p: exag and df.
 template <typename T, int D>
-__global__ void __launch_bounds__(kBlock) k_kl(const uint32_t *__restrict__ row, const uint32_t *__restrict__ col,
-                                               const T *__restrict__ val, const T *__restrict__ Y, int N,
-                                               double exag, double dfd, RedScratch r) {
-    __shared__ double sh[32];
-    kl_body<T, D>(row, col, val, Y, 0, N, exag, dfd, r, sh, blockIdx.x, gridDim.x);
+__global__ void __launch_bounds__(kBlock, 4) k_kl_rows(const uint32_t *__restrict__ row,
+                                                       const uint32_t *__restrict__ col, const T *__restrict__ val,
+                                                       const T *__restrict__ Y, int N, UpdateParams p, RedScratch r) {
+    __shared__ double sh[2 * 32];
+    __shared__ int block_item;
+    attr_body<T, D, 16, 2, false, false, true>(row, col, val, Y, nullptr, nullptr, nullptr, nullptr, nullptr, 0, N, p,
+                                               r, nullptr, sh, &block_item, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------------
@@ -1724,11 +1757,26 @@ cudaError_t launch_attr_tiles_update(const uint2 *trec, const uint32_t *tstart, 
 template <typename T>
 cudaError_t launch_kl(const uint32_t *row, const uint32_t *col, const T *val, const T *Y, int N, int D, double exag,
                       double df, RedScratch r, cudaStream_t st) {
-    const int g = grid_for((long long) N * 32, kBlock, kRedGrid);
+    UpdateParams p{};
+    p.exag = exag;
+    p.df = df;
+    // one resident wave: the warps take row groups from the work counter
+    static int wave[2] = {0, 0};
+    int &w = wave[D == 2 ? 1 : 0];
+    if (w == 0) {
+        int dev = 0, nsm = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const cudaError_t e = D == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_kl_rows<T, 2>, kBlock, 0)
+                                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_kl_rows<T, 1>, kBlock, 0);
+        if (e != cudaSuccess) return e;
+        w = std::min(kMaxRedBlocks, nsm * (per_sm > 0 ? per_sm : 1));
+    }
+    const int g = grid_for(((long long) N + 31) / 32 * 32, kBlock, w);
     if (D == 2)
-        k_kl<T, 2><<<g, kBlock, 0, st>>>(row, col, val, Y, N, exag, df, r);
+        k_kl_rows<T, 2><<<g, kBlock, 0, st>>>(row, col, val, Y, N, p, r);
     else
-        k_kl<T, 1><<<g, kBlock, 0, st>>>(row, col, val, Y, N, exag, df, r);
+        k_kl_rows<T, 1><<<g, kBlock, 0, st>>>(row, col, val, Y, N, p, r);
     return cudaGetLastError();
 }
 
