@@ -146,8 +146,9 @@ int fitsne_session_get_y(fitsne_session *s, double *Y);
  * of the whole last fitsne_session_run call (CUDA events on the session's stream),
  * out[9] = number of kernels that call launched. */
 int fitsne_session_set_timing(fitsne_session *s, int on);
-/* 1 (default unless FITSNE_GRAPH=0): iterations run as graph-captured chunks with the grid
- * sized on the device; 0: one host round trip per iteration (the per-stage timing path). */
+/* 1 (default unless FITSNE_GRAPH=0): iterations run in chunks of replayed two-iteration CUDA
+ * graphs with the grid sized on the device; 0: one host round trip per iteration (the
+ * per-stage timing path). */
 int fitsne_session_set_graphs(fitsne_session *s, int on);
 int fitsne_session_stage_times(fitsne_session *s, double *out10);
 /* Launch shapes the session's autotuner chose (no reference counterpart), out[5]: the
