@@ -593,38 +593,66 @@ FITSNE_D void spread_runs_body(const float *__restrict__ Y, int N, const BoxP<fl
             }
         }
         if constexpr (D == 2) {
-            // run sums through the warp's table: lane l stores its 9 node charges in column l;
-            // lane q < 9 then adds up row q (node q) in point order and, at the end of each run,
-            // issues that node's float4 atomic for the run's box
+            // run sums through the warp's table: lane l stores its 9 node charges in column l.
+            // Then 27 lanes add up the table, lane (q, j) = (lane % 9, lane / 9) node q over
+            // the points of range j ([0, 11), [11, 22), [22, 32)) in order: a run that ends
+            // inside the range and began there is issued at once (one float4 atomic for the
+            // run's box); the first run end of a range also closes the run carried in from the
+            // ranges before, whose pieces (the earlier ranges' tails) come by shuffles.  A warp's
+            // run ends (`ends`, lane 31 always) are the same for every lane.
             const int next = __shfl_down_sync(full, key, 1);
             const unsigned ends = __ballot_sync(full, lane == 31 || next != key);
 #pragma unroll
             for (int q = 0; q < NV; ++q) wb->v[q][lane] = make_float4(v[q][0], v[q][1], v[q][2], v[q][3]);
             wb->cell[lane] = valid ? (long long) bx[0] * NT * b.M + (long long) bx[1] * NT : -1ll;
             __syncwarp();
-            if (lane < NV) {
-                const long long off = (long long) (lane / NT) * b.M + lane % NT;
-                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                // eight points' loads issued together, then added in order: one shared-memory
-                // latency per eight points instead of per point
-#pragma unroll 1
-                for (int g = 0; g < 32; g += 8) {
-                    float4 x[8];
+            const int q = lane % NV, j = lane / NV;  // lanes 27 - 31: j = 3, no range
+            const int lo = 11 * j, n = j < 2 ? 11 : (j == 2 ? 10 : 0);
+            const long long off = (long long) (q / NT) * b.M + q % NT;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f), head = acc;
+            int first_end = -1;
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) x[k] = wb->v[lane][g + k];
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        acc.x += x[k].x;
-                        acc.y += x[k].y;
-                        acc.z += x[k].z;
-                        acc.w += x[k].w;
-                        if ((ends >> (g + k)) & 1u) {
-                            const long long c = wb->cell[g + k];
+            for (int k = 0; k < 11; ++k) {
+                if (k < n) {
+                    const int pt = lo + k;
+                    const float4 x = wb->v[q][pt];
+                    acc.x += x.x;
+                    acc.y += x.y;
+                    acc.z += x.z;
+                    acc.w += x.w;
+                    if ((ends >> pt) & 1u) {
+                        if (first_end < 0) {
+                            first_end = pt;  // closes the run carried in: issued after the join
+                            head = acc;
+                        } else {
+                            const long long c = wb->cell[pt];
                             if (c >= 0) atomicAdd(reinterpret_cast<float4 *>(grid + c + off), acc);
-                            acc = make_float4(0.f, 0.f, 0.f, 0.f);
                         }
+                        acc = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
                 }
+            }
+            // acc is now this range's tail (the part of a run that goes on past the range).
+            // The run closed at range j's first end began in range j, or earlier: its earlier
+            // pieces are range j - 1's tail and, when range j - 1 has no run end, range j - 2's.
+            const int s1 = lane >= NV ? lane - NV : lane, s2 = lane >= 2 * NV ? lane - 2 * NV : lane;
+            const float4 t1 = make_float4(__shfl_sync(full, acc.x, s1), __shfl_sync(full, acc.y, s1),
+                                          __shfl_sync(full, acc.z, s1), __shfl_sync(full, acc.w, s1));
+            const float4 t2 = make_float4(__shfl_sync(full, acc.x, s2), __shfl_sync(full, acc.y, s2),
+                                          __shfl_sync(full, acc.z, s2), __shfl_sync(full, acc.w, s2));
+            if (first_end >= 0) {
+                float4 carry = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j >= 1) carry = t1;
+                if (j == 2 && (ends & (0x7ffu << 11)) == 0u) {  // range 1 has no run end
+                    carry.x += t2.x;
+                    carry.y += t2.y;
+                    carry.z += t2.z;
+                    carry.w += t2.w;
+                }
+                const float4 run = make_float4(carry.x + head.x, carry.y + head.y, carry.z + head.z,
+                                               carry.w + head.w);
+                const long long c = wb->cell[first_end];
+                if (c >= 0) atomicAdd(reinterpret_cast<float4 *>(grid + c + off), run);
             }
             __syncwarp();  // the table is rewritten by the next 32 points
         } else {
