@@ -39,9 +39,9 @@ struct GridGeom {
     float s32[kMaxInterp], inv_den32[kMaxInterp];
     double s64[kMaxInterp], inv_den64[kMaxInterp];
     // FP32 forms for the FP32 kernels: -mn and bw as double-float (hi, lo) pairs, 1 / bw
-    // rounded to float.  Made once here: every thread of the spread and gather used to derive
-    // them itself, ~20 FP64-pipe instructions a warp at ~16 cycles each (about 30 us a launch
-    // over 31,250 warps at N = 1M).
+    // rounded to float.  Made once here instead of by every thread of the spread and gather
+    // (FP64 conversions and a division on the FP64 pipe; the gather at N = 1M went from 0.034
+    // to 0.031 ms).
     float neg_mn32[2], bw32[2], inv_bw32;
 };
 
