@@ -62,10 +62,17 @@ def test_run_random_init_uses_the_reference_generator(gpu_lib):
 
 def test_run_leaves_the_data_unmodified(gpu_lib):
     """fitsne_run reads X without centring or rescaling it in place (the reference does both to
-    its own copy), so the wrapper passes the caller's array without copying it."""
+    its own copy): called through the C ABI on the caller's array, which must come back as it
+    went in."""
     X = np.random.default_rng(1).standard_normal((500, 6)) * 3.0 + 1.0
     X0 = X.copy()
-    gpu_lib.run(X, perplexity=10.0, rand_seed=3, max_iter=5)
+    Y = np.zeros((500, 2))
+    c = np.zeros(5)
+    dp = ctypes.POINTER(ctypes.c_double)
+    rc = gpu_lib.lib().fitsne_run(X.ctypes.data_as(dp), 500, 6, Y.ctypes.data_as(dp), 2, 10.0, 0.5, 3, 0, 5, 250,
+                                  250, .5, .8, 200.0, -1, -1.0, 2, 2, 12.0, c.ctypes.data_as(dp), 0, -1, -1.0, 50,
+                                  -1, 3, 1.0, 50, 0, 0, 0, None, 1.0, 5.0)
+    assert rc == 0 and np.isfinite(Y).all()
     assert np.array_equal(X, X0)
 
 
