@@ -395,7 +395,8 @@ FITSNE_D bool grid_minmax_pairs(float nh, float nl, float xh, float xl, double &
 template <typename T, int D>
 FITSNE_D void center_minmax_body(T *Y, int N, int apply_mean, int excl, RedScratch r, double *sh, int blk, int nblk) {
     typedef typename YL<T, D>::P P;
-    // -mean in the positions' form, made by thread 0 (FP64 conversions: see step_scalars)
+    // -mean in the positions' form, made by thread 0 (FP64 conversions, ~16 cycles a warp
+    // instruction on GB300's FP64 pipe, once per block instead of once per warp)
     __shared__ P s_negm[D];
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -777,42 +778,14 @@ __global__ void __launch_bounds__(kBlock) k_gather(const T *__restrict__ Y, int 
 // repulsion over Z; tsne.cpp:1121-1155) and, in mode 1, the reference's update (gains,
 // momentum, step clipping; tsne.cpp:479-531) into Yout, the new position added to msum; in
 // mode 0 the gradient into dC only.
-// The step's scalars in the kernel's type, made once per block by thread 0 (the FP64
-// division and conversions cost every warp that made them ~16 cycles a warp instruction on
-// GB300's FP64 pipe, all at the start of the launch).  Called by every thread of the block.
-template <typename T>
-struct StepScalars {
-    T zinv, exag, df, momentum, lr, max_step;
-    bool df1, clip;
-};
-template <typename T>
-FITSNE_D StepScalars<T> step_scalars(const UpdateParams &p, const double *z) {
-    __shared__ StepScalars<T> sc;
-    if (threadIdx.x == 0) {
-        sc.zinv = T(1.0 / *z);
-        sc.exag = T(p.exag);
-        sc.df = T(p.df);
-        sc.momentum = T(p.momentum);
-        sc.lr = T(p.learning_rate);
-        sc.max_step = T(p.max_step_norm);
-        sc.df1 = p.df == 1.0;
-        sc.clip = p.max_step_norm > 0;
-    }
-    __syncthreads();
-    const StepScalars<T> v = sc;
-    __syncthreads();  // a later call may rewrite sc
-    return v;
-}
-
 template <typename T, int D>
 FITSNE_D void attr_row_update(int my, const T (&amy)[D], const typename YL<T, D>::P (&cmy)[D], const UpdateParams &p,
-                              const StepScalars<T> &sc, const T *__restrict__ rep, T *__restrict__ dC,
-                              T *__restrict__ gains, T *__restrict__ uY, T *__restrict__ Yout,
-                              typename YL<T, D>::P (&msum)[D]) {
+                              T zinv, T exag, const T *__restrict__ rep, T *__restrict__ dC, T *__restrict__ gains,
+                              T *__restrict__ uY, T *__restrict__ Yout, typename YL<T, D>::P (&msum)[D]) {
     typedef typename YL<T, D>::P P;
     T gr[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) gr[d] = sc.exag * amy[d] - rep[(size_t) my * D + d] * sc.zinv;
+    for (int d = 0; d < D; ++d) gr[d] = exag * amy[d] - rep[(size_t) my * D + d] * zinv;
     if (p.mode == 0) {
 #pragma unroll
         for (int d = 0; d < D; ++d) dC[(size_t) my * D + d] = gr[d];
@@ -829,15 +802,15 @@ FITSNE_D void attr_row_update(int my, const T (&amy)[D], const typename YL<T, D>
             gn = (sgn(gr[d]) != sgn(uo)) ? (gn + T(0.2)) : (gn * T(0.8));
             if (gn < T(0.01)) gn = T(0.01);
             gains[(size_t) my * D + d] = gn;
-            u[d] = sc.momentum * uo - sc.lr * gn * gr[d];
+            u[d] = T(p.momentum) * uo - T(p.learning_rate) * gn * gr[d];
             nrm2 += u[d] * u[d];
         }
-        if (sc.clip) {
+        if (p.max_step_norm > 0) {
             const T step = sqrt(nrm2);
-            if (step > sc.max_step) {
-                const T f = sc.max_step / step;
+            if (step > T(p.max_step_norm)) {
+                const T sc = T(p.max_step_norm) / step;
 #pragma unroll
-                for (int d = 0; d < D; ++d) u[d] *= f;
+                for (int d = 0; d < D; ++d) u[d] *= sc;
             }
         }
 #pragma unroll
@@ -921,9 +894,11 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
     const int lane = threadIdx.x & 31;
     const int ngroups = (N + kAttrGroup - 1) / kAttrGroup;
     const unsigned int nwarps = (nblk * blockDim.x) >> 5;
-    const StepScalars<T> sc = step_scalars<T>(p, r.z);
-    const T df = sc.df;
-    const bool df1 = sc.df1;
+    const double Zd = *r.z;
+    const T zinv = T(1.0 / Zd);
+    const T df = T(p.df);
+    const bool df1 = (p.df == 1.0);
+    const T exag = T(p.exag);
     P msum[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) {
@@ -1058,8 +1033,8 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
                     }
                     const T q = recip(df1 ? T(1) + d2 : T(1) + d2 / df);
                     if constexpr (kKL) {
-                        const T Q = (df1 ? q : pow(q, df)) * sc.zinv;
-                        const T pv = v[u] * sc.exag;
+                        const T Q = (df1 ? q : pow(q, df)) * zinv;
+                        const T pv = v[u] * exag;
                         a[0] += pv * log((pv + T(FLT_MIN)) / (Q + T(FLT_MIN)));  // 0 past the row
                     } else {
                         const T vq = v[u] * q;
@@ -1079,7 +1054,7 @@ FITSNE_D void attr_body(const uint32_t *__restrict__ row, const uint32_t *__rest
             }
         }
         if (kKL || !live) continue;
-        attr_row_update<T, D>(my, amy, cmy, p, sc, rep, dC, gains, uY, Yout, msum);
+        attr_row_update<T, D>(my, amy, cmy, p, zinv, exag, rep, dC, gains, uY, Yout, msum);
     }
     if constexpr (kKL) {
         if (lane == 0) {  // the work counter's reset, as attr_finish does it
@@ -1193,7 +1168,8 @@ __global__ void __launch_bounds__(kBlock)
                  const float *__restrict__ rep, int N, UpdateParams p, RedScratch r) {
     __shared__ double sh[2 * 32];
     typedef df32 P;
-    const StepScalars<float> sc = step_scalars<float>(p, r.z);
+    const float zinv = (float) (1.0 / *r.z);
+    const float exag = (float) p.exag;
     P msum[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) msum[d] = {0.f, 0.f};
@@ -1210,7 +1186,7 @@ __global__ void __launch_bounds__(kBlock)
         }
         P cmy[D];
         YL<float, D>::load(Yin, i, cmy);
-        attr_row_update<float, D>(i, amy, cmy, p, sc, rep, dC, gains, uY, Yout, msum);
+        attr_row_update<float, D>(i, amy, cmy, p, zinv, exag, rep, dC, gains, uY, Yout, msum);
     }
     if (p.mode != 0) {
         double m[2] = {0.0, 0.0};
